@@ -1,0 +1,101 @@
+/*
+ * vmc_gb300.h — C ABI of the GB300 VMC inner-loop library (libvmc_gb300.so).
+ *
+ * Every entry point takes raw device pointers, sizes and a cudaStream_t (passed
+ * as void*), enqueues work on that stream and returns a status code; it never
+ * allocates, frees or synchronises caller memory.  Host wrappers turn status
+ * codes into the reference's exceptions.
+ *
+ * Walker layout: occ[2*w] = up bits, occ[2*w+1] = down bits (site i -> bit i,
+ * n_sites <= 64).  Configurations at the API boundary use the reference's
+ * quimb encoding {0: empty, 1: down, 2: up, 3: up+down} as int64 (B, n_sites).
+ *
+ * Reference interfaces replaced (paths within sjdu10/vmc_torch):
+ *   vmc_pack / vmc_unpack        — quimb <-> netket conversion,
+ *                                  vmc_torch/fermion_utils.py:1448-1498 and the
+ *                                  inline form in vmc_torch/GPU/models/slater.py:53-56
+ *   vmc_init_walkers             — random_initial_config, vmc_torch/GPU/vmc_utils.py:22-39;
+ *                                  initialize_walkers, vmc_torch/GPU/vmc_setup.py:139-159
+ *   vmc_hubbard_conn             — SpinfulFermionGPUMixin.get_conn_batch_gpu,
+ *                                  vmc_torch/hamiltonian_torch.py:586-655
+ *   vmc_slater_refresh           — SlaterDeterminant_GPU.amplitude / forward_log,
+ *                                  vmc_torch/GPU/models/slater.py:40-61, _base.py:101-130
+ *   vmc_slater_sweep             — MetropolisExchangeSpinfulSamplerGPU.step,
+ *                                  vmc_torch/GPU/sampler.py:217-388 (+ proposals 47-137)
+ *   vmc_slater_local_energy      — _evaluate_energy_impl, vmc_torch/GPU/vmc_utils.py:322-476
+ *   vmc_slater_logpsi_grad       — compute_grads_gpu, vmc_torch/GPU/vmc_utils.py:1389-1634
+ *   vmc_sr_*                     — minSR_solver_gpu, vmc_torch/GPU/optimizer.py:471-614
+ *   vmc_energy_gradient          — the run_sr=False branch, vmc_torch/GPU/optimizer.py:585-613
+ */
+#ifndef VMC_GB300_H
+#define VMC_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum vmc_status {
+  VMC_OK = 0,
+  VMC_ERR_ARGS = 1,        /* invalid sizes / null pointers / unsupported shape */
+  VMC_ERR_CUDA = 2,        /* a launch failed */
+  VMC_ERR_NONFINITE = 3,   /* non-finite amplitude or energy */
+  VMC_ERR_SINGULAR = 4,    /* singular orbital matrix */
+  VMC_ERR_TIMEOUT = 5,     /* a bounded device-side wait gave up */
+  VMC_ERR_UNSUPPORTED = 6  /* configuration not built into this library */
+};
+
+int vmc_abi_version(void);
+
+/* ---- walkers and the Hubbard connected set ---- */
+/* fxs (B, n_sites) int64 quimb -> occ (B, 2) uint64.  *d_bad (device int) is set
+ * to 1 when a value is outside {0,1,2,3}. */
+int vmc_pack(const int64_t* fxs, int64_t B, int n_sites, uint64_t* occ, int* d_bad, void* stream);
+int vmc_unpack(const uint64_t* occ, int64_t B, int n_sites, int64_t* fxs, void* stream);
+/* Seeded uniform random sector states (n_up up, n_dn down electrons). */
+int vmc_init_walkers(uint64_t* occ, int64_t B, int n_sites, int n_up, int n_dn, uint64_t seed, void* stream);
+/* Connected set, T = 2*n_edges + n_sites slots per walker: for each edge (order
+ * of `edges`, int32 [n_edges][2]) spin up then spin down, then one on-site slot
+ * per site.  eta (B, T, 2) uint64, coeff (B, T) float64, valid (B, T) uint8. */
+int vmc_hubbard_conn(const uint64_t* occ, int64_t B, int n_sites, const int32_t* edges, int n_edges, double t,
+                     double U, uint64_t* eta, double* coeff, uint8_t* valid, void* stream);
+
+/* ---- Slater determinant (FP64): psi(x) = det(M[ascending occupied rows]) ----
+ * M (n_orb = 2*n_sites, nf) row-major float64.  Per-walker state: G (B, nf, nf)
+ * float64 with G[k][c] = (A^-1)[c][k]; slot_orb (B, nf) uint8; sign, logabs (B)
+ * float64; n_acc (B) int32 accepted moves since the last re-inversion. */
+int vmc_slater_refresh(const double* M, int n_orb, int nf, const uint64_t* occ, int64_t B, int n_sites, double* G,
+                       uint8_t* slot_orb, double* sign, double* logabs, int32_t* n_acc, int threshold,
+                       int* d_n_singular, void* stream);
+/* n_sweeps sweeps over `edges` (sweep order).  Random stream: replay buffers
+ * r_move/r_bit/r_acc of shape (n_sweeps, n_edges, B) when non-null, else
+ * Philox4x32-10 keyed by seed with counter (walker, sweep_offset + s, edge). */
+int vmc_slater_sweep(const double* M, int n_orb, int nf, uint64_t* occ, int64_t B, int n_sites, const int32_t* edges,
+                     int n_edges, int n_sweeps, float hopping_rate, uint64_t seed, uint64_t sweep_offset,
+                     const float* r_move, const uint8_t* r_bit, const float* r_acc, double* G, uint8_t* slot_orb,
+                     double* sign, double* logabs, int32_t* n_acc, void* stream);
+int vmc_slater_local_energy(const double* M, int n_orb, int nf, const uint64_t* occ, int64_t B, int n_sites,
+                            const int32_t* edges, int n_edges, double t, double U, const double* G,
+                            const uint8_t* slot_orb, double* eloc, void* stream);
+/* O (B, ldo) float64, O[w][o*nf + c] = d log|psi| / d M[o][c]. */
+int vmc_slater_logpsi_grad(const double* G, const uint8_t* slot_orb, int64_t B, int n_orb, int nf, double* O,
+                           int64_t ldo, void* stream);
+
+/* ---- minSR in sample space (dtype: 0 = float64, 1 = float32 for O / Oc) ---- */
+int vmc_sr_center(const void* O, int dtype, int64_t Ns, int64_t Np, int64_t ldo, void* Oc, int64_t ldc, double* mean,
+                  void* stream);
+int vmc_sr_gram(const void* Oc, int dtype, int64_t Ns, int64_t Np, int64_t ldc, double* T, int64_t ldt,
+                double diag_shift, int accumulate, void* stream);
+int vmc_sr_cholesky(double* T, int64_t n, int64_t ldt, int* d_info, void* stream);
+int vmc_sr_cholesky_solve(const double* L, int64_t n, int64_t ldt, double* b, void* stream);
+int vmc_sr_rhs(const double* E, int64_t Ns, double Ebar, double* b, void* stream);
+int vmc_sr_update(const void* Oc, int dtype, int64_t Ns, int64_t Np, int64_t ldc, const double* x, double* dp,
+                  void* stream);
+int vmc_energy_gradient(const void* O, int dtype, int64_t Ns, int64_t Np, int64_t ldo, const double* E, double Ebar,
+                        double* g, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VMC_GB300_H */

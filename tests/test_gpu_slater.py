@@ -1,0 +1,180 @@
+"""GPU parity of the walker, Hubbard and Slater kernels against the oracle and
+the reference's golden vectors.  Tolerances: configurations, connected sets and
+signs bit-exact; FP64 amplitudes, local energies and O within 1e-10 relative."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import hubbard, lattice, models, sampler as osampler, sr
+import vmc_torch_gb300 as vg
+
+pytestmark = pytest.mark.gpu
+DEV = "cuda"
+
+
+def canonical_from_torch(etas, coeffs, bids, B):
+    pk = lattice.pack(etas.cpu().numpy())
+    c = coeffs.cpu().numpy()
+    b = bids.cpu().numpy()
+    rows = []
+    for w in range(B):
+        m = np.nonzero(b == w)[0]
+        rows.extend((w,) + k for k in sorted((int(pk[q, 0]), int(pk[q, 1]), float(c[q])) for q in m))
+    return rows
+
+
+def test_pack_unpack_roundtrip():
+    X = lattice.random_initial_configs(300, 64, 32, 32, seed=3)
+    x = torch.as_tensor(X, device=DEV)
+    occ = vg.pack(x)
+    ref = lattice.pack(X)
+    assert np.array_equal(occ.cpu().numpy().view(np.uint64), ref)
+    assert torch.equal(vg.unpack(occ, 64), x)
+    bad = x.clone()
+    bad[0, 0] = 7
+    with pytest.raises(ValueError):
+        vg.pack(bad)
+
+
+def test_init_walkers_sector():
+    x = vg.init_walkers(1000, 36, 16, 16, seed=9).cpu().numpy()
+    nk = lattice.quimb_to_netket(x)
+    assert (nk[:, :36].sum(1) == 16).all() and (nk[:, 36:].sum(1) == 16).all()
+    assert len({tuple(r) for r in x}) > 990
+
+
+@pytest.mark.parametrize("case", ["4x2", "8x8"])
+def test_connected_set_bit_exact(golden, case):
+    g = golden("conn.npz")
+    if case == "4x2":
+        X, Lx, Ly, nps = g["states_4x2"].astype(np.int64), 4, 2, (4, 4)
+    else:
+        X, Lx, Ly, nps = g["x_8x8"].astype(np.int64), 8, 8, (32, 32)
+    H = vg.spinful_Fermi_Hubbard_square_lattice_torch(Lx, Ly, 1.0, 8.0, sum(nps), n_fermions_per_spin=nps)
+    H.precompute_hops_gpu(DEV)
+    e, c, b = H.get_conn_batch_gpu(torch.as_tensor(X, device=DEV))
+    mine = canonical_from_torch(e, c, b, len(X))
+    ref = [(int(bb), int(u), int(d), float(cc)) for bb, (u, d), cc in
+           zip(g[f"bid_{case}"], g[f"pk_{case}"], g[f"coeff_{case}"])]
+    assert mine == ref
+    # term-major order identical to the oracle's restatement of get_conn_batch_gpu
+    oe, oc, ob = hubbard.get_conn_batch(X, lattice.square_edges(Lx, Ly), 1.0, 8.0)
+    assert np.array_equal(e.cpu().numpy(), oe) and np.array_equal(b.cpu().numpy(), ob)
+    assert np.array_equal(c.cpu().numpy(), oc)
+
+
+def _slater(M):
+    m = vg.SlaterDeterminant_GB300(M.shape[0], M.shape[1]).to(DEV)
+    with torch.no_grad():
+        m.params[0].copy_(torch.as_tensor(M))
+    m.invalidate()
+    return m
+
+
+def test_slater_amplitudes_match_reference(golden):
+    g = golden("slater.npz")
+    S = golden("conn.npz")["states_4x2"].astype(np.int64)
+    m = _slater(g["M"])
+    amp = m(torch.as_tensor(S, device=DEV)).cpu().numpy()
+    np.testing.assert_allclose(amp, g["amps_all"], rtol=1e-10, atol=0)
+
+
+def test_slater_replayed_sweep_matches_reference(golden):
+    g = golden("slater.npz")
+    m = _slater(g["M"])
+    H = vg.spinful_Fermi_Hubbard_square_lattice_torch(4, 2, 1.0, 8.0, 8, n_fermions_per_spin=(4, 4))
+    H.precompute_hops_gpu(DEV)
+    smp = vg.MetropolisExchangeSpinfulSamplerGB300()
+    fx = torch.as_tensor(g["x0"], device=DEV).clone()
+    for s in range(3):
+        rp = tuple(torch.as_tensor(a[s:s + 1], device=DEV).contiguous() for a in (g["u_move"], g["hop_bit"], g["u_acc"]))
+        fx, amps = smp.step(fx, m, H.graph, replay=rp)
+    assert np.array_equal(fx.cpu().numpy(), g["x_final"])
+    np.testing.assert_allclose(amps.cpu().numpy(), g["amps_final"], rtol=1e-10)
+    _, eloc = vg.evaluate_energy(fx, m, H, amps)
+    np.testing.assert_allclose(eloc.cpu().numpy(), g["eloc"], rtol=1e-10, atol=1e-10)
+    O, a2 = vg.compute_grads_gpu(fx, m, use_log_amp=True)
+    np.testing.assert_allclose(O.cpu().numpy(), g["O"], rtol=1e-10, atol=1e-12)
+    graw, amps2 = vg.compute_grads_gpu(fx, m)
+    np.testing.assert_allclose((graw / amps2[:, None]).cpu().numpy(), g["O"], rtol=1e-9, atol=1e-12)
+
+
+@pytest.mark.parametrize("Lx,Ly,nup,B,S", [(4, 2, 4, 256, 4), (4, 4, 7, 128, 3), (8, 8, 32, 32, 2)])
+def test_slater_sweep_vs_oracle_replay(Lx, Ly, nup, B, S):
+    N = Lx * Ly
+    rng = np.random.default_rng(Lx * 100 + Ly)
+    M = rng.normal(0, 0.1, size=(2 * N, 2 * nup))
+    m = _slater(M)
+    g = vg.SquareLattice(Lx, Ly)
+    E = len(g.sweep_edges())
+    X = lattice.random_initial_configs(B, N, nup, nup, seed=N)
+    um = rng.random((S, E, B), dtype=np.float32)
+    hb = rng.integers(0, 2, (S, E, B)).astype(np.uint8)
+    ua = rng.random((S, E, B), dtype=np.float32)
+    xo, (so, lo), nacc = osampler.sweep(X, lattice.sweep_edges(Lx, Ly), lambda y: models.slater_logamp(M, y), um, hb, ua)
+    smp = vg.MetropolisExchangeSpinfulSamplerGB300()
+    fx = torch.as_tensor(X, device=DEV).clone()
+    rp = tuple(torch.as_tensor(a, device=DEV).contiguous() for a in (um, hb, ua))
+    fx = smp.burn_in(fx, m, g, S, replay=rp)
+    assert np.array_equal(fx.cpu().numpy(), xo)
+    st = m.bind_state(fx)
+    assert np.array_equal(st.sign.cpu().numpy(), so)
+    np.testing.assert_allclose(st.logabs.cpu().numpy(), lo, rtol=1e-10, atol=1e-9)
+    # local energy and O after the sweeps, FP64 within 1e-10
+    H = vg.spinful_Fermi_Hubbard_square_lattice_torch(Lx, Ly, 1.0, 8.0, 2 * nup, n_fermions_per_spin=(nup, nup))
+    H.precompute_hops_gpu(DEV)
+    _, eloc = vg.evaluate_energy(fx, m, H)
+    ref = hubbard.local_energy(xo, lattice.square_edges(Lx, Ly), 1.0, 8.0, lambda y: models.slater_amp(M, y))
+    np.testing.assert_allclose(eloc.cpu().numpy(), ref, rtol=1e-10, atol=1e-9)
+    O, _ = vg.compute_grads_gpu(fx, m, use_log_amp=True)
+    np.testing.assert_allclose(O.cpu().numpy(), models.slater_O(M, xo), rtol=1e-9, atol=1e-10)
+
+
+def test_minsr_matches_reference(golden):
+    g = golden("minsr.npz")
+    solver = vg.MinSRGB300()
+    dp, _, info = solver.solve(local_o=torch.as_tensor(g["O"], device=DEV), local_energies=torch.as_tensor(g["E"], device=DEV),
+                               energy_mean=float(g["E"].mean()), total_samples=64, n_params=96,
+                               diag_shift=float(g["diag_shift"]), device=DEV, run_sr=True)
+    assert info == 0
+    np.testing.assert_allclose(dp.cpu().numpy(), g["dp"], rtol=1e-9, atol=1e-12)
+    gr, _, _ = solver.solve(local_o=torch.as_tensor(g["O"], device=DEV), local_energies=torch.as_tensor(g["E"], device=DEV),
+                            energy_mean=float(g["E"].mean()), total_samples=64, n_params=96,
+                            diag_shift=1e-4, device=DEV, run_sr=False)
+    np.testing.assert_allclose(gr.cpu().numpy(), sr.energy_gradient(g["O"], g["E"], g["E"].mean()), rtol=1e-10, atol=1e-13)
+
+
+def test_minsr_large_vs_oracle():
+    rng = np.random.default_rng(5)
+    O = rng.standard_normal((700, 300)) * 0.2
+    E = rng.standard_normal(700)
+    dp, _, info = vg.MinSRGB300().solve(local_o=torch.as_tensor(O, device=DEV), local_energies=torch.as_tensor(E, device=DEV),
+                                        energy_mean=float(E.mean()), total_samples=700, n_params=300, diag_shift=1e-3,
+                                        device=DEV, run_sr=True)
+    np.testing.assert_allclose(dp.cpu().numpy(), sr.minsr(O, E, E.mean(), 1e-3), rtol=1e-8, atol=1e-10)
+
+
+def test_vmc_4x2_reaches_exact_energy_of_its_parameters():
+    """Config 1 slice: 4x2 Slater VMC with minSR; the MC energy agrees with the
+    exact <H> of the same parameters, which lies above the ED ground state."""
+    torch.manual_seed(0)
+    gen = torch.Generator().manual_seed(0)
+    H = vg.spinful_Fermi_Hubbard_square_lattice_torch(4, 2, 1.0, 8.0, 8, n_fermions_per_spin=(4, 4))
+    H.precompute_hops_gpu(DEV)
+    model = vg.SlaterDeterminant_GB300(16, 8, init_std=0.1, generator=gen).to(DEV)
+    smp = vg.MetropolisExchangeSpinfulSamplerGB300(seed=1, sweeps_per_step=2)
+    fx = vg.init_walkers(1024, 8, 4, 4, seed=2)
+    cfg = vg.VMCLoopConfig(vmc_steps=30, ns_per_rank=1024, grad_batch_size=1024, n_params=128, nsites=8,
+                           learning_rate=0.1, diag_shift=1e-4, burn_in_steps=50, outlier_clip_factor=0.0)
+    drv = vg.VMC_GB300(smp, vg.MinSRGB300(), vg.SGDGB300(0.1))
+    fx, hist = drv.run_vmc_loop(fx, model, H, H.graph, cfg)
+    assert hist[-1]["energy"] < hist[0]["energy"] - 1.0
+    S, Hd = hubbard.dense_hamiltonian(8, 4, 4, lattice.square_edges(4, 2), 1.0, 8.0)
+    for _ in range(10):
+        fx, _ = smp.step(fx, model, H.graph)
+    M = model.params[0].detach().cpu().numpy()
+    Eex = hubbard.exact_energy(models.slater_amp(M, S), Hd)
+    _, eloc = vg.evaluate_energy(fx, model, H)
+    e = eloc.cpu().numpy()
+    assert abs(e.mean() - Eex) < 5 * e.std() / np.sqrt(len(e)) + 0.05
+    assert Eex > -3.025922805691 - 1e-9

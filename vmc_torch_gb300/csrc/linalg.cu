@@ -1,0 +1,294 @@
+// Sample-space SR (minSR) linear algebra on one GPU:
+//   column means and centring/scaling of O, the Gram matrix T = O~ O~^T + lambda I,
+//   a blocked right-looking FP64 Cholesky of T, forward/backward substitution,
+//   and dp = O~^T x.  Also the plain energy gradient <E O> - <E><O>.
+#include "common.cuh"
+
+namespace {
+
+constexpr int TB = 64;   // output tile
+constexpr int TK = 16;   // k chunk
+
+// mean[p] = (1/Ns) sum_i O[i][p];  Oc[i][p] = (O[i][p] - mean[p]) * scale
+template <typename TI, typename TO>
+__global__ void k_center(const TI* __restrict__ O, int64_t Ns, int64_t Np, int64_t ldo, TO* __restrict__ Oc,
+                         int64_t ldc, double* __restrict__ mean, double scale) {
+  int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= Np) return;
+  double s = 0.0;
+  for (int64_t i = 0; i < Ns; ++i) s += (double)O[i * ldo + p];
+  const double m = s / (double)Ns;
+  if (mean) mean[p] = m;
+  if (Oc)
+    for (int64_t i = 0; i < Ns; ++i) Oc[i * ldc + p] = (TO)(((double)O[i * ldo + p] - m) * scale);
+}
+
+// g[p] = (1/Ns) sum_i E[i] O[i][p] - Ebar * mean_i O[i][p]
+template <typename TI>
+__global__ void k_egrad(const TI* __restrict__ O, int64_t Ns, int64_t Np, int64_t ldo, const double* __restrict__ E,
+                        double Ebar, double* __restrict__ g) {
+  int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= Np) return;
+  double se = 0.0, so = 0.0;
+  for (int64_t i = 0; i < Ns; ++i) {
+    double o = (double)O[i * ldo + p];
+    se += E[i] * o;
+    so += o;
+  }
+  g[p] = se / (double)Ns - Ebar * so / (double)Ns;
+}
+
+// C[i][j] (+)= sign * sum_{k<K} A[i][k] * A[j][k] for lower-triangular 64x64 tiles
+// (tile row >= tile col).  A row-major with leading dim lda; rows offset by
+// row0 for both operands; columns of C offset by col0 as well.  Tiles of the
+// strict upper triangle are mirrored when mirror != 0.
+template <typename TI, typename TA>
+__global__ void k_syrk(const TI* __restrict__ A, int64_t lda, int64_t n, int64_t K, double* __restrict__ C,
+                       int64_t ldc, int64_t off, double sgn, double diag, int mirror) {
+  const int bi = blockIdx.y, bj = blockIdx.x;
+  if (bj > bi) return;
+  __shared__ TA As[TK][TB + 1];
+  __shared__ TA Bs[TK][TB + 1];
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  const int64_t i0 = off + (int64_t)bi * TB, j0 = off + (int64_t)bj * TB;
+  TA acc[4][4] = {};
+  for (int64_t k0 = 0; k0 < K; k0 += TK) {
+    for (int idx = threadIdx.x; idx < TB * TK; idx += 256) {
+      int r = idx / TK, kk = idx - r * TK;
+      int64_t gk = k0 + kk;
+      int64_t gi = i0 + r, gj = j0 + r;
+      As[kk][r] = (gi < off + n && gk < K) ? (TA)A[gi * lda + gk] : (TA)0;
+      Bs[kk][r] = (gj < off + n && gk < K) ? (TA)A[gj * lda + gk] : (TA)0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < TK; ++kk) {
+      TA a[4], b[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) { a[q] = As[kk][ty * 4 + q]; b[q] = Bs[kk][tx * 4 + q]; }
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+#pragma unroll
+        for (int r = 0; r < 4; ++r) acc[q][r] += a[q] * b[r];
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      int64_t gi = i0 + ty * 4 + q, gj = j0 + tx * 4 + r;
+      if (gi < off + n && gj < off + n && gj <= gi) {
+        double v = C[gi * ldc + gj] + sgn * (double)acc[q][r];
+        if (gi == gj) v += diag;
+        C[gi * ldc + gj] = v;
+        if (mirror && gi != gj) C[gj * ldc + gi] = v;
+      }
+    }
+}
+
+// Unblocked Cholesky of one diagonal tile (lower), in place; flags non-positive pivots.
+__global__ void k_potrf_tile(double* __restrict__ C, int64_t ldc, int64_t k0, int64_t nb, int* __restrict__ info) {
+  __shared__ double a[TB][TB + 1];
+  for (int idx = threadIdx.x; idx < nb * nb; idx += blockDim.x) {
+    int r = idx / nb, c = idx - r * nb;
+    a[r][c] = C[(k0 + r) * ldc + k0 + c];
+  }
+  __syncthreads();
+  for (int k = 0; k < nb; ++k) {
+    if (threadIdx.x == 0) {
+      double d = a[k][k];
+      if (!(d > 0.0) || !isfinite(d)) { atomicExch(info, 1); d = 1e-300; }
+      a[k][k] = sqrt(d);
+    }
+    __syncthreads();
+    for (int r = k + 1 + threadIdx.x; r < nb; r += blockDim.x) a[r][k] /= a[k][k];
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < nb * nb; idx += blockDim.x) {
+      int r = idx / nb, c = idx - r * nb;
+      if (c > k && r >= c) a[r][c] -= a[r][k] * a[c][k];
+    }
+    __syncthreads();
+  }
+  for (int idx = threadIdx.x; idx < nb * nb; idx += blockDim.x) {
+    int r = idx / nb, c = idx - r * nb;
+    C[(k0 + r) * ldc + k0 + c] = (c <= r) ? a[r][c] : 0.0;
+  }
+}
+
+// Panel: X = A21 * L11^{-T} for the rows below the diagonal tile; one thread per row.
+__global__ void k_trsm_panel(double* __restrict__ C, int64_t ldc, int64_t n, int64_t k0, int64_t nb) {
+  __shared__ double L[TB][TB + 1];
+  for (int idx = threadIdx.x; idx < nb * nb; idx += blockDim.x) {
+    int r = idx / nb, c = idx - r * nb;
+    L[r][c] = C[(k0 + r) * ldc + k0 + c];
+  }
+  __syncthreads();
+  int64_t row = k0 + nb + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= n) return;
+  double x[TB];
+  double* a = C + row * ldc + k0;
+  for (int k = 0; k < nb; ++k) {
+    double v = a[k];
+    for (int m = 0; m < k; ++m) v -= x[m] * L[k][m];
+    x[k] = v / L[k][k];
+  }
+  for (int k = 0; k < nb; ++k) a[k] = x[k];
+}
+
+// Single-block triangular solves with the lower factor L (ld ldc):
+// trans = 0: L y = b;  trans = 1: L^T x = b.  In place on b.
+__global__ void k_trsv(const double* __restrict__ L, int64_t ldc, int64_t n, double* __restrict__ b, int trans) {
+  if (!trans) {
+    for (int64_t j = 0; j < n; ++j) {
+      __syncthreads();
+      double xj = b[j] / L[j * ldc + j];
+      __syncthreads();
+      if (threadIdx.x == 0) b[j] = xj;
+      for (int64_t i = j + 1 + threadIdx.x; i < n; i += blockDim.x) b[i] -= L[i * ldc + j] * xj;
+    }
+  } else {
+    for (int64_t j = n - 1; j >= 0; --j) {
+      __syncthreads();
+      double xj = b[j] / L[j * ldc + j];
+      __syncthreads();
+      if (threadIdx.x == 0) b[j] = xj;
+      for (int64_t i = threadIdx.x; i < j; i += blockDim.x) b[i] -= L[j * ldc + i] * xj;
+    }
+  }
+}
+
+// dp[p] = sum_i Oc[i][p] * x[i]
+template <typename TI>
+__global__ void k_gemv_t(const TI* __restrict__ Oc, int64_t Ns, int64_t Np, int64_t ldc, const double* __restrict__ x,
+                         double* __restrict__ dp) {
+  int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= Np) return;
+  double s = 0.0;
+  for (int64_t i = 0; i < Ns; ++i) s += (double)Oc[i * ldc + p] * x[i];
+  dp[p] = s;
+}
+
+__global__ void k_rhs(const double* __restrict__ E, int64_t Ns, double Ebar, double scale, double* __restrict__ b) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < Ns) b[i] = (E[i] - Ebar) * scale;
+}
+
+__global__ void k_zero(double* __restrict__ p, int64_t n) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) p[i] = 0.0;
+}
+
+}  // namespace
+
+extern "C" {
+
+// Centre and scale O (Ns x Np, ld ldo) into Oc (ld ldc): Oc = (O - mean)/sqrt(Ns).
+// dtype codes: 0 = float64, 1 = float32 (for both O and Oc).
+int vmc_sr_center(const void* O, int dtype, int64_t Ns, int64_t Np, int64_t ldo, void* Oc, int64_t ldc, double* mean,
+                  void* stream) {
+  if (Ns <= 0 || Np <= 0 || ldo < Np || ldc < Np || !O || !Oc) return VMC_ERR_ARGS;
+  const double scale = 1.0 / sqrt((double)Ns);
+  unsigned grid = (unsigned)((Np + 255) / 256);
+  if (dtype == 0)
+    k_center<double, double><<<grid, 256, 0, (cudaStream_t)stream>>>((const double*)O, Ns, Np, ldo, (double*)Oc, ldc,
+                                                                      mean, scale);
+  else if (dtype == 1)
+    k_center<float, float><<<grid, 256, 0, (cudaStream_t)stream>>>((const float*)O, Ns, Np, ldo, (float*)Oc, ldc,
+                                                                    mean, scale);
+  else
+    return VMC_ERR_ARGS;
+  VMC_CUDA_CHECK_LAUNCH();
+  return VMC_OK;
+}
+
+// T (Ns x Ns, FP64, ld ldt) = (accumulate ? T : 0) + Oc Oc^T (+ diag_shift on the diagonal).
+int vmc_sr_gram(const void* Oc, int dtype, int64_t Ns, int64_t Np, int64_t ldc, double* T, int64_t ldt,
+                double diag_shift, int accumulate, void* stream) {
+  if (Ns <= 0 || Np < 0 || ldc < Np || ldt < Ns || !Oc || !T) return VMC_ERR_ARGS;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (!accumulate) {
+    int64_t n = Ns * ldt;
+    k_zero<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(T, n);
+  }
+  int64_t nt = (Ns + TB - 1) / TB;
+  if (nt > 65535) return VMC_ERR_ARGS;
+  dim3 grid((unsigned)nt, (unsigned)nt);
+  if (dtype == 0)
+    k_syrk<double, double><<<grid, 256, 0, s>>>((const double*)Oc, ldc, Ns, Np, T, ldt, 0, 1.0, diag_shift, 1);
+  else if (dtype == 1)
+    k_syrk<float, float><<<grid, 256, 0, s>>>((const float*)Oc, ldc, Ns, Np, T, ldt, 0, 1.0, diag_shift, 1);
+  else
+    return VMC_ERR_ARGS;
+  VMC_CUDA_CHECK_LAUNCH();
+  return VMC_OK;
+}
+
+// In-place lower Cholesky of T (FP64).  d_info set to 1 on a non-positive pivot.
+int vmc_sr_cholesky(double* T, int64_t n, int64_t ldt, int* d_info, void* stream) {
+  if (n <= 0 || ldt < n || !T || !d_info) return VMC_ERR_ARGS;
+  cudaStream_t s = (cudaStream_t)stream;
+  for (int64_t k0 = 0; k0 < n; k0 += TB) {
+    int64_t nb = (n - k0) < TB ? (n - k0) : TB;
+    k_potrf_tile<<<1, 256, 0, s>>>(T, ldt, k0, nb, d_info);
+    int64_t rest = n - k0 - nb;
+    if (rest > 0) {
+      k_trsm_panel<<<(unsigned)((rest + 63) / 64), 64, 0, s>>>(T, ldt, n, k0, nb);
+      int64_t nt = (rest + TB - 1) / TB;
+      dim3 grid((unsigned)nt, (unsigned)nt);
+      // trailing update of the lower triangle: A22 -= L21 L21^T
+      k_syrk<double, double><<<grid, 256, 0, s>>>(T + k0, ldt, rest, nb, T, ldt, k0 + nb, -1.0, 0.0, 0);
+    }
+  }
+  VMC_CUDA_CHECK_LAUNCH();
+  return VMC_OK;
+}
+
+// Solve L L^T x = b in place on b (L from vmc_sr_cholesky).
+int vmc_sr_cholesky_solve(const double* L, int64_t n, int64_t ldt, double* b, void* stream) {
+  if (n <= 0 || ldt < n || !L || !b) return VMC_ERR_ARGS;
+  k_trsv<<<1, 1024, 0, (cudaStream_t)stream>>>(L, ldt, n, b, 0);
+  k_trsv<<<1, 1024, 0, (cudaStream_t)stream>>>(L, ldt, n, b, 1);
+  VMC_CUDA_CHECK_LAUNCH();
+  return VMC_OK;
+}
+
+// b = (E - Ebar)/sqrt(Ns)
+int vmc_sr_rhs(const double* E, int64_t Ns, double Ebar, double* b, void* stream) {
+  if (Ns <= 0 || !E || !b) return VMC_ERR_ARGS;
+  k_rhs<<<(unsigned)((Ns + 255) / 256), 256, 0, (cudaStream_t)stream>>>(E, Ns, Ebar, 1.0 / sqrt((double)Ns), b);
+  VMC_CUDA_CHECK_LAUNCH();
+  return VMC_OK;
+}
+
+// dp = Oc^T x
+int vmc_sr_update(const void* Oc, int dtype, int64_t Ns, int64_t Np, int64_t ldc, const double* x, double* dp,
+                  void* stream) {
+  if (Ns <= 0 || Np <= 0 || ldc < Np || !Oc || !x || !dp) return VMC_ERR_ARGS;
+  unsigned grid = (unsigned)((Np + 255) / 256);
+  if (dtype == 0)
+    k_gemv_t<double><<<grid, 256, 0, (cudaStream_t)stream>>>((const double*)Oc, Ns, Np, ldc, x, dp);
+  else if (dtype == 1)
+    k_gemv_t<float><<<grid, 256, 0, (cudaStream_t)stream>>>((const float*)Oc, Ns, Np, ldc, x, dp);
+  else
+    return VMC_ERR_ARGS;
+  VMC_CUDA_CHECK_LAUNCH();
+  return VMC_OK;
+}
+
+// g = <E O> - Ebar <O>
+int vmc_energy_gradient(const void* O, int dtype, int64_t Ns, int64_t Np, int64_t ldo, const double* E, double Ebar,
+                        double* g, void* stream) {
+  if (Ns <= 0 || Np <= 0 || ldo < Np || !O || !E || !g) return VMC_ERR_ARGS;
+  unsigned grid = (unsigned)((Np + 255) / 256);
+  if (dtype == 0)
+    k_egrad<double><<<grid, 256, 0, (cudaStream_t)stream>>>((const double*)O, Ns, Np, ldo, E, Ebar, g);
+  else if (dtype == 1)
+    k_egrad<float><<<grid, 256, 0, (cudaStream_t)stream>>>((const float*)O, Ns, Np, ldo, E, Ebar, g);
+  else
+    return VMC_ERR_ARGS;
+  VMC_CUDA_CHECK_LAUNCH();
+  return VMC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,209 @@
+"""Wavefunction models with the reference's model interface
+(vmc_torch/GPU/models/_base.py:21-142): ``forward(x) -> (B,)`` amplitudes,
+``forward_log(x) -> (signs, log_abs)``, single-sample ``amplitude(x,
+params_list)`` and ``params`` (an ``nn.ParameterList`` whose flattened order is
+the column order of O).
+
+Behind the interface every evaluation runs in libvmc_gb300 kernels.  A model
+keeps one persistent walker state (packed occupations plus the per-walker
+amplitude data the kernels update in place) bound to the configuration tensor
+it last saw; sampler, local energy and gradients share it.
+"""
+import torch
+import torch.nn as nn
+
+from . import _lib
+from .walkers import pack, unpack
+
+
+class WalkerState:
+    """Device buffers for B walkers, bound to one (B, N) config tensor."""
+
+    def __init__(self, B, n_sites, device):
+        self.B, self.n_sites, self.device = B, n_sites, device
+        self.occ = torch.empty((B, 2), dtype=torch.int64, device=device)
+        self.sign = torch.empty(B, dtype=torch.float64, device=device)
+        self.logabs = torch.empty(B, dtype=torch.float64, device=device)
+        self.n_acc = torch.zeros(B, dtype=torch.int32, device=device)
+        self.key = None          # (data_ptr, _version, shape) of the bound config tensor
+        self.param_key = None    # model parameter fingerprint at the last refresh
+        self.extra = {}
+
+    def bound_to(self, fxs):
+        return self.key == (fxs.data_ptr(), fxs._version, tuple(fxs.shape))
+
+    def bind(self, fxs):
+        self.key = (fxs.data_ptr(), fxs._version, tuple(fxs.shape))
+
+
+class WavefunctionModel_GB300(nn.Module):
+    """Base class: parameter list, state binding and the log/amp dispatch."""
+
+    def __init__(self, params_list, n_sites):
+        super().__init__()
+        self.params = nn.ParameterList([p if isinstance(p, nn.Parameter) else nn.Parameter(p) for p in params_list])
+        self.n_sites = n_sites
+        self._state = None
+        self._bump = 0
+
+    # ---- parameter bookkeeping ----
+    def invalidate(self):
+        """Call after changing parameters through ``.data`` (which torch does not
+        version-count); the optimizers in this package call it themselves."""
+        self._bump += 1
+
+    def param_key(self):
+        return (self._bump,) + tuple((p.data_ptr(), p._version) for p in self.params)
+
+    @property
+    def n_params(self):
+        return sum(p.numel() for p in self.params)
+
+    # ---- state management ----
+    def _new_state(self, B, device):
+        return WalkerState(B, self.n_sites, device)
+
+    def bind_state(self, fxs):
+        """Return the walker state for ``fxs``, re-packing and re-evaluating the
+        amplitudes when fxs or the parameters changed since the last use."""
+        _lib.require_cuda(fxs, "fxs")
+        if fxs.dim() != 2 or fxs.shape[1] != self.n_sites:
+            raise ValueError("fxs must be (B, %d) int64" % self.n_sites)
+        st = self._state
+        pk = self.param_key()
+        if st is not None and st.B == fxs.shape[0] and st.device == fxs.device and st.bound_to(fxs) \
+                and st.param_key == pk:
+            return st
+        if st is None or st.B != fxs.shape[0] or st.device != fxs.device:
+            st = self._new_state(fxs.shape[0], fxs.device)
+            self._state = st
+        st.occ.copy_(pack(fxs))
+        self._refresh(st, threshold=0)
+        st.bind(fxs)
+        st.param_key = pk
+        return st
+
+    def _eval_state(self, x):
+        """A fresh state for arbitrary configs (not bound)."""
+        st = self._new_state(x.shape[0], x.device)
+        st.occ.copy_(pack(x))
+        self._refresh(st, threshold=0)
+        return st
+
+    def store_configs(self, st, fxs):
+        """Write the state's configurations into fxs in place and re-bind."""
+        unpack(st.occ, self.n_sites, out=fxs)
+        st.bind(fxs)
+
+    # ---- reference interface ----
+    def forward_log(self, x):
+        if x.shape[0] == 0:
+            z = torch.zeros(0, dtype=torch.float64, device=x.device)
+            return z, z.clone()
+        st = self._eval_state(x)
+        return st.sign.clone(), st.logabs.clone()
+
+    def forward(self, x):
+        s, la = self.forward_log(x)
+        return s * torch.exp(la)
+
+    def log_amplitude(self, x, params_list=None):
+        s, la = self.forward_log(x.reshape(1, -1))
+        return s[0], la[0]
+
+    def amplitude(self, x, params_list=None):
+        """Single-sample amplitude (the model's current parameters are used; the
+        reference passes them explicitly for torch.func transforms, which this
+        library replaces with hand-written adjoints)."""
+        return self.forward(x.reshape(1, -1))[0]
+
+    # ---- hooks implemented by subclasses ----
+    def _refresh(self, st, threshold):
+        raise NotImplementedError
+
+    def sweep(self, st, graph, n_sweeps, seed, sweep_offset, hopping_rate=0.25, replay=None):
+        raise NotImplementedError
+
+    def local_energy(self, st, H):
+        raise NotImplementedError
+
+    def logpsi_grad(self, st):
+        raise NotImplementedError
+
+
+class SlaterDeterminant_GB300(WavefunctionModel_GB300):
+    """psi(x) = det(M[ascending occupied rows]), M of shape (2N, N_f), FP64
+    (vmc_torch/GPU/models/slater.py:15-61; ascending rows as in
+    vmc_torch/model.py:7437-7457).
+
+    ``init_std`` scales the N(0, 1) init of the reference (``torch.randn``);
+    ``generator`` seeds it."""
+
+    def __init__(self, n_orbitals, n_fermions, dtype=torch.float64, init_std=1.0, generator=None,
+                 refresh_every=64):
+        if dtype != torch.float64:
+            raise ValueError("the Slater walker kernels run in FP64")
+        if n_fermions > 64 or n_orbitals > 128 or n_orbitals % 2:
+            raise ValueError("supports n_fermions <= 64 and n_orbitals = 2 * n_sites <= 128")
+        M = torch.randn(n_orbitals, n_fermions, dtype=dtype, generator=generator) * init_std
+        super().__init__([M], n_orbitals // 2)
+        self.n_fermions = n_fermions
+        self.n_orbitals = n_orbitals
+        self.refresh_every = refresh_every
+
+    def _new_state(self, B, device):
+        st = WalkerState(B, self.n_sites, device)
+        nf = self.n_fermions
+        st.extra["G"] = torch.empty((B, nf, nf), dtype=torch.float64, device=device)
+        st.extra["slot"] = torch.empty((B, nf), dtype=torch.uint8, device=device)
+        st.extra["nsing"] = torch.zeros(1, dtype=torch.int32, device=device)
+        return st
+
+    def _M(self, device):
+        M = self.params[0]
+        if M.device != device:
+            raise ValueError("model parameters must live on the walkers' device (call model.to(device))")
+        return M.detach().contiguous()
+
+    def _refresh(self, st, threshold):
+        M = self._M(st.device)
+        _lib.call("vmc_slater_refresh", _lib.ptr(M), self.n_orbitals, self.n_fermions, _lib.ptr(st.occ), st.B,
+                  self.n_sites, _lib.ptr(st.extra["G"]), _lib.ptr(st.extra["slot"]), _lib.ptr(st.sign),
+                  _lib.ptr(st.logabs), _lib.ptr(st.n_acc), int(threshold), _lib.ptr(st.extra["nsing"]),
+                  _lib.stream_of(st.device))
+
+    def sweep(self, st, graph, n_sweeps, seed, sweep_offset, hopping_rate=0.25, replay=None):
+        from .hamiltonian import device_sweep_edges
+        M = self._M(st.device)
+        edges = device_sweep_edges(graph, st.device)
+        rm = rb = ra = None
+        if replay is not None:
+            rm, rb, ra = replay
+            E = edges.shape[0]
+            for a in (rm, rb, ra):
+                if tuple(a.shape) != (n_sweeps, E, st.B) or not a.is_cuda or not a.is_contiguous():
+                    raise ValueError("replay buffers must be contiguous CUDA tensors of shape (n_sweeps, E, B)")
+        _lib.call("vmc_slater_sweep", _lib.ptr(M), self.n_orbitals, self.n_fermions, _lib.ptr(st.occ), st.B,
+                  self.n_sites, _lib.ptr(edges), edges.shape[0], int(n_sweeps), float(hopping_rate),
+                  int(seed) & ((1 << 64) - 1), int(sweep_offset), _lib.ptr(rm), _lib.ptr(rb), _lib.ptr(ra),
+                  _lib.ptr(st.extra["G"]), _lib.ptr(st.extra["slot"]), _lib.ptr(st.sign), _lib.ptr(st.logabs),
+                  _lib.ptr(st.n_acc), _lib.stream_of(st.device))
+        if self.refresh_every:
+            self._refresh(st, threshold=self.refresh_every)
+
+    def local_energy(self, st, H):
+        M = self._M(st.device)
+        edges = H.edges_on(st.device)
+        eloc = torch.empty(st.B, dtype=torch.float64, device=st.device)
+        _lib.call("vmc_slater_local_energy", _lib.ptr(M), self.n_orbitals, self.n_fermions, _lib.ptr(st.occ), st.B,
+                  self.n_sites, _lib.ptr(edges), edges.shape[0], float(H.t), float(H.U), _lib.ptr(st.extra["G"]),
+                  _lib.ptr(st.extra["slot"]), _lib.ptr(eloc), _lib.stream_of(st.device))
+        return eloc
+
+    def logpsi_grad(self, st, out=None):
+        Np = self.n_params
+        if out is None:
+            out = torch.empty((st.B, Np), dtype=torch.float64, device=st.device)
+        _lib.call("vmc_slater_logpsi_grad", _lib.ptr(st.extra["G"]), _lib.ptr(st.extra["slot"]), st.B,
+                  self.n_orbitals, self.n_fermions, _lib.ptr(out), out.stride(0), _lib.stream_of(st.device))
+        return out
