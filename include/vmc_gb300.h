@@ -82,6 +82,51 @@ int vmc_slater_local_energy(const double* M, int n_orb, int nf, const uint64_t* 
 int vmc_slater_logpsi_grad(const double* G, const uint8_t* slot_orb, int64_t B, int n_orb, int nf, double* O,
                            int64_t ldo, void* stream);
 
+/* ---- Neural-network backflow (NNBF_GPU, vmc_torch/GPU/models/NNBF.py:36-162) ----
+ * psi(x) = det((M_base + s * (out_w h2(x) + out_b))[ascending occupied rows]),
+ * h2 = gelu(W1 gelu(W0 n + b0) + b1), hidden width 256, two hidden layers.
+ * prec 0 ("mixed"): BF16 tensor-core GEMMs (tcgen05, FP32 accumulate), FP32 LU,
+ *   log|det| combined in FP64; requires nf in {32, 64} and 2*n_sites*nf % 256 == 0.
+ * prec 1 ("fp64"): every stage in FP64 on CUDA cores (parity mode).
+ * net_ptrs[7] (device pointers), prec 0 / prec 1 element types:
+ *   [0] W0^T (2N, 256) f32/f64   [1] b0 (256) f32/f64   [2] W1 (256, 256) bf16/f64
+ *   [3] b1 (256) f32/f64          [4] out_w (2N*nf, 256) bf16/f64
+ *   [5] out_b (2N*nf) f32/f64     [6] M_base (2N, nf) f32/f64
+ * Workspace for R rows (caller-owned): H1, H2 (R, 256) bf16/f64; A (R, nf, nf) f32/f64.
+ * d_err (device int) receives VMC_ERR_TIMEOUT if a bounded device wait gave up. */
+/* Evaluate R configurations from scratch: sign/logabs (R), and z0 = W0 n + b0
+ * (R, 256) f32/f64 when z0_out is non-null.  Replaces forward_log / vamp_log
+ * (vmc_torch/GPU/models/_base.py:101-130). */
+int vmc_nnbf_eval(int prec, const void* const* net_ptrs, int n_sites, int nf, int hidden, double bf_scale,
+                  const uint64_t* occ, int64_t R, void* z0_out, void* H1, void* H2, void* A, double* sign,
+                  double* logabs, int* d_err, void* stream);
+/* Metropolis sweeps (MetropolisExchangeSpinfulSamplerGPU.step,
+ * vmc_torch/GPU/sampler.py:217-388): per edge, propose for all B walkers,
+ * evaluate every proposal, accept with min(1, |psi'|^2/|psi|^2).  Walker state
+ * occ, z0 (B, 256), sign, logabs, n_acc is updated in place.  Workspace:
+ * prop_occ (B, 2) u64, rec (B, 16 bytes), H1/H2/A for B rows.  Random stream as
+ * in vmc_slater_sweep. */
+int vmc_nnbf_sweep(int prec, const void* const* net_ptrs, int n_sites, int nf, int hidden, double bf_scale,
+                   uint64_t* occ, int64_t B, const int32_t* edges, int n_edges, int n_sweeps, float hopping_rate,
+                   uint64_t seed, uint64_t sweep_offset, const float* r_move, const uint8_t* r_bit, const float* r_acc,
+                   void* z0, double* sign, double* logabs, int32_t* n_acc, uint64_t* prop_occ, void* rec, void* H1,
+                   void* H2, void* A, int* d_err, void* stream);
+/* Local-energy support (vmc_torch/GPU/vmc_utils.py:322-476): per-walker count
+ * of valid hop terms, then the (walker, hop-term) pair list at offsets offs
+ * (B+1, exclusive scan of the counts).  Hop term = 2*edge + (0 up, 1 down). */
+int vmc_nnbf_conn_count(const uint64_t* occ, int64_t B, int n_sites, const int32_t* edges, int n_edges, int32_t* cnt,
+                        void* stream);
+int vmc_nnbf_conn_pairs(const uint64_t* occ, int64_t B, int n_sites, const int32_t* edges, int n_edges,
+                        const int32_t* offs, int32_t* pairs, void* stream);
+/* E_loc(x) = U * doublons + sum_pairs H_{x,eta} psi(eta)/psi(x), evaluating
+ * `chunk` connected configurations at a time with workspace row_occ (chunk, 2),
+ * coeff (chunk), H1/H2/A for chunk rows; term (P) holds the per-pair terms. */
+int vmc_nnbf_local_energy(int prec, const void* const* net_ptrs, int n_sites, int nf, int hidden, double bf_scale,
+                          const uint64_t* occ, int64_t B, const int32_t* edges, double t, double U, const void* z0,
+                          const double* sign, const double* logabs, const int32_t* pairs, const int32_t* offs,
+                          int64_t P, int64_t chunk, uint64_t* row_occ, double* coeff, double* term, void* H1, void* H2,
+                          void* A, double* eloc, int* d_err, void* stream);
+
 /* ---- minSR in sample space (dtype: 0 = float64, 1 = float32 for O / Oc) ---- */
 int vmc_sr_center(const void* O, int dtype, int64_t Ns, int64_t Np, int64_t ldo, void* Oc, int64_t ldc, double* mean,
                   void* stream);

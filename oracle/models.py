@@ -57,12 +57,6 @@ def slater_O(M, x):
     return O.reshape(B, -1)
 
 
-_ACT = {
-    "gelu": lambda z: 0.5 * z * (1.0 + np.vectorize(math.erf)(z / math.sqrt(2.0))),
-    "tanh": np.tanh,
-}
-
-
 def gelu_np(z):
     from scipy.special import erf
     return 0.5 * z * (1.0 + erf(z / math.sqrt(2.0)))
@@ -145,3 +139,24 @@ def nnbf_init(n_sites, n_f, hidden, n_layers, seed, bf_scale_std=None):
     ps.append(g.normal(0.0, 1.0 / math.sqrt(fan), size=(n_orb * n_f, fan)))
     ps.append(np.zeros(n_orb * n_f))
     return ps
+
+
+def nnbf_logamp_bf16(params, x, bf_scale):
+    """CPU emulation of the GB300 mixed-precision NNBF path: W1, out_w, h1 and
+    h2 rounded to BF16, everything else FP32, exact (FP64) determinant of the
+    resulting FP32 orbital matrix.  Separates the BF16 quantisation error (a
+    property of the mixed path) from kernel errors."""
+    def bf16(a):
+        return torch.as_tensor(np.asarray(a, np.float32)).to(torch.bfloat16).to(torch.float32).numpy()
+
+    M_base, w0, b0, w1, b1, out_w, out_b = [np.asarray(p, np.float64) for p in params]
+    f32 = np.float32
+    n = quimb_to_netket(np.asarray(x)).astype(f32)
+    z0 = n @ w0.T.astype(f32) + b0.astype(f32)
+    h1 = bf16(gelu_np(z0.astype(np.float64)))
+    h2 = bf16(gelu_np((h1 @ bf16(w1).T + b1.astype(f32)).astype(np.float64)))
+    dM = (h2 @ bf16(out_w).T).astype(f32) + out_b.astype(f32)
+    M = M_base.astype(f32)[None] + f32(bf_scale) * dM.reshape(-1, *M_base.shape)
+    rows = occupied_rows(x)
+    A = np.take_along_axis(M, rows[:, :, None], axis=1).astype(np.float64)
+    return np.linalg.slogdet(A)

@@ -1,0 +1,133 @@
+"""GPU parity of the neural-backflow path.
+
+fp64 mode: log-amplitudes, replayed sweeps and local energies against the
+reference's golden vectors and the oracle within 1e-10 relative; configurations
+and signs bit-exact.
+mixed mode (BF16 tensor-core MLP, FP32 determinant): |log|psi| - oracle| <=
+5e-3 + 1e-5 * cond(A) per configuration (A = the FP64 orbital matrix; BF16
+rounding of the MLP, ~1e-5 relative on A, is amplified by the condition number
+near nodes), identical signs where cond(A) < 1e4; local energies within 1e-2
+relative; a replayed sweep reproduces the oracle's configurations for >= 95 %
+of the walkers (acceptance decisions within the precision of the mixed path
+may flip)."""
+import hashlib
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import hubbard, lattice, models as om, sampler as osampler
+import vmc_torch_gb300 as vg
+
+pytestmark = pytest.mark.gpu
+DEV = "cuda"
+LOG_TOL_MIXED = 5e-3
+
+
+def fixture_params(g):
+    ps = om.nnbf_init(64, 64, 256, 2, seed=int(g["seed"]))
+    h = hashlib.sha256()
+    for p in ps:
+        h.update(np.ascontiguousarray(p, dtype=np.float64).tobytes())
+    return ps, h.hexdigest() == str(g["params_sha256"])
+
+
+def make_model(ps, n_sites, nf, precision):
+    m = vg.NNBF_GB300(n_sites, nf, precision=precision).to(DEV)
+    with torch.no_grad():
+        for p, v in zip(m.params, ps):
+            p.copy_(torch.as_tensor(v))
+    m.invalidate()
+    return m
+
+
+def test_fp64_logamp_matches_reference(golden):
+    g = golden("nnbf.npz")
+    ps, same = fixture_params(g)
+    m = make_model(ps, 64, 64, "fp64")
+    X = g["x"].astype(np.int64)
+    s, l = m.forward_log(torch.as_tensor(X, device=DEV))
+    so, lo = om.nnbf_logamp(ps, X, 0.01)
+    assert np.array_equal(s.cpu().numpy(), so)
+    np.testing.assert_allclose(l.cpu().numpy(), lo, rtol=1e-10, atol=1e-10)
+    if same:
+        assert np.array_equal(s.cpu().numpy(), g["sign"])
+        np.testing.assert_allclose(l.cpu().numpy(), g["logabs"], rtol=1e-10, atol=1e-10)
+
+
+def test_fp64_replayed_sweep_and_energy_match_reference(golden):
+    g = golden("nnbf.npz")
+    ps, same = fixture_params(g)
+    if not same:
+        pytest.skip("numpy normal stream differs from the one that made the fixture")
+    m = make_model(ps, 64, 64, "fp64")
+    H = vg.spinful_Fermi_Hubbard_square_lattice_torch(8, 8, 1.0, 8.0, 64, n_fermions_per_spin=(32, 32))
+    H.precompute_hops_gpu(DEV)
+    fx = torch.as_tensor(g["x0"].astype(np.int64), device=DEV).clone()
+    rp = tuple(torch.as_tensor(a, device=DEV).contiguous() for a in (g["u_move"], g["hop_bit"], g["u_acc"]))
+    smp = vg.MetropolisExchangeSpinfulSamplerGB300()
+    fx, (s, l) = smp.step(fx, m, H.graph, use_log_amp=True, replay=rp)
+    assert np.array_equal(fx.cpu().numpy(), g["x_final"].astype(np.int64))
+    assert np.array_equal(s.cpu().numpy(), g["sign_final"])
+    np.testing.assert_allclose(l.cpu().numpy(), g["logabs_final"], rtol=1e-10, atol=1e-10)
+    _, eloc = vg.evaluate_energy(fx, m, H, (s, l), use_log_amp=True)
+    np.testing.assert_allclose(eloc.cpu().numpy(), g["eloc"], rtol=1e-10, atol=1e-9)
+
+
+@pytest.mark.parametrize("Lx,Ly,nup,B", [(8, 8, 32, 300), (6, 6, 16, 200)])
+def test_mixed_logamp_vs_fp64_oracle(Lx, Ly, nup, B):
+    N = Lx * Ly
+    nf = 2 * nup
+    ps = om.nnbf_init(N, nf, 256, 2, seed=N + nf)
+    X = lattice.random_initial_configs(B, N, nup, nup, seed=7)
+    so, lo = om.nnbf_logamp(ps, X, 0.01)
+    m = make_model(ps, N, nf, "mixed")
+    s, l = m.forward_log(torch.as_tensor(X, device=DEV))
+    s, l = s.cpu().numpy(), l.cpu().numpy()
+    err = np.abs(l - lo)
+    Mx = om.nnbf_M(ps, X, 0.01)
+    cond = np.linalg.cond(np.take_along_axis(Mx, om.occupied_rows(X)[:, :, None], axis=1))
+    print("mixed log|psi| abs err: max %.3e median %.3e; max err at cond<1e3: %.3e"
+          % (err.max(), np.median(err), err[cond < 1e3].max()))
+    assert np.array_equal(s[cond < 1e4], so[cond < 1e4])
+    assert np.median(err) < 2e-3
+    assert (err <= LOG_TOL_MIXED + 1e-4 * cond).all()
+    # against the CPU emulation of the BF16 path itself: only FP32 LU / GELU rounding differences remain
+    sb, lb = om.nnbf_logamp_bf16(ps, X, 0.01)
+    eb = np.abs(l - lb)
+    print("mixed vs BF16-path emulation: max %.3e median %.3e" % (eb.max(), np.median(eb)))
+    assert np.median(eb) < 2e-4
+    assert (eb <= 2e-3 + 2e-6 * cond).all()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_sweep_and_local_energy_vs_oracle(precision):
+    Lx, Ly, nup, B, S = 6, 6, 16, 48, 2
+    N, nf = Lx * Ly, 2 * nup
+    ps = om.nnbf_init(N, nf, 256, 2, seed=123)
+    rng = np.random.default_rng(4)
+    E = lattice.sweep_edges(Lx, Ly)
+    X = lattice.random_initial_configs(B, N, nup, nup, seed=8)
+    um = rng.random((S, len(E), B), dtype=np.float32)
+    hb = rng.integers(0, 2, (S, len(E), B)).astype(np.uint8)
+    ua = rng.random((S, len(E), B), dtype=np.float32)
+    xo, (so, lo), _ = osampler.sweep(X, E, lambda y: om.nnbf_logamp(ps, y, 0.01), um, hb, ua)
+    m = make_model(ps, N, nf, precision)
+    g = vg.SquareLattice(Lx, Ly)
+    fx = torch.as_tensor(X, device=DEV).clone()
+    rp = tuple(torch.as_tensor(a, device=DEV).contiguous() for a in (um, hb, ua))
+    fx = vg.MetropolisExchangeSpinfulSamplerGB300().burn_in(fx, m, g, S, replay=rp)
+    same = (fx.cpu().numpy() == xo).all(axis=1)
+    if precision == "fp64":
+        assert same.all()
+    else:
+        assert same.mean() >= 0.95
+    H = vg.spinful_Fermi_Hubbard_square_lattice_torch(Lx, Ly, 1.0, 8.0, nf, n_fermions_per_spin=(nup, nup))
+    H.precompute_hops_gpu(DEV)
+    _, eloc = vg.evaluate_energy(fx, m, H)
+    xg = fx.cpu().numpy()
+    ref = hubbard.local_energy(xg, lattice.square_edges(Lx, Ly), 1.0, 8.0, lambda y: om.nnbf_amp(ps, y, 0.01))
+    if precision == "fp64":
+        np.testing.assert_allclose(eloc.cpu().numpy(), ref, rtol=1e-10, atol=1e-9)
+    else:
+        np.testing.assert_allclose(eloc.cpu().numpy(), ref, rtol=1e-2, atol=1e-2)

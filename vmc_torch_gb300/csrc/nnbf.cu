@@ -1,0 +1,1145 @@
+// Neural-network backflow (NNBF) amplitudes on GB300.
+//
+//   n = [up | dn] (2N spin-orbitals);  z0 = W0 n + b0;  h1 = gelu(z0);
+//   h2 = gelu(W1 h1 + b1);  dM = out_w h2 + out_b  (2N x nf);
+//   M = M_base + s * dM;  psi = det(M[ascending occupied rows])
+//
+// Evaluation pipeline over R "rows" (a row = one configuration to evaluate:
+// a proposal during a sweep, a connected configuration during the local
+// energy, or a walker's current configuration on refresh):
+//   prep      : z0(row) from the walker's z0 plus the moved orbitals' W0
+//               columns (or from scratch), h1 = gelu(z0) -> H1 (bf16 / fp64)
+//   layer1    : H2 = gelu(H1 W1^T + b1)            tcgen05 GEMM 128x256x256
+//   backflow  : A[row][pos] = M_base[r] + s (H2 out_w[r]^T + out_b[r]) for each
+//               occupied orbital r at ascending position pos
+//                                                   tcgen05 GEMM 128x256x256,
+//               gather of occupied rows fused in the epilogue
+//   logdet    : LU with partial pivoting, one warp per row, FP32 registers;
+//               |det| accumulated as a normalised mantissa and an integer
+//               exponent, combined in FP64; then Metropolis accept / local
+//               energy term / refresh, fused.
+// An FP64 twin of every stage (CUDA cores) gives the 1e-10 parity mode.
+#include <cuda_bf16.h>
+#include <utility>
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include "common.cuh"
+#include "tc.cuh"
+
+using namespace vmc;
+
+namespace {
+
+constexpr int HID = 256;
+constexpr int TM = 128;          // rows per GEMM tile
+constexpr int TN = 256;          // output columns per GEMM tile
+constexpr int SMEM_A = TM * HID * 2;   // 64 KB
+constexpr int SMEM_B = TN * HID * 2;   // 128 KB
+constexpr int GEMM_SMEM = SMEM_A + SMEM_B + 1024 /*align*/ + 64 + 2 * TN * 4;
+
+__device__ __forceinline__ float gelu_f(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
+__device__ __forceinline__ double gelu_d(double x) { return 0.5 * x * (1.0 + erf(x * 0.70710678118654752440)); }
+
+// Proposal record (one per walker for sweeps): flag, packed moves, n moves, u_acc
+struct __align__(16) PropRec {
+  int flag;
+  int moves;  // a0 | b0 << 8 | a1 << 16 | b1 << 24
+  int nmov;
+  float u_acc;
+};
+
+__device__ __forceinline__ void unpack_moves(const PropRec& r, int* a, int* b) {
+  a[0] = r.moves & 0xff; b[0] = (r.moves >> 8) & 0xff; a[1] = (r.moves >> 16) & 0xff; b[1] = (r.moves >> 24) & 0xff;
+}
+
+// ---------------------------------------------------------------------------
+// prep kernels (warp per row, lane handles 8 consecutive hidden units)
+// ---------------------------------------------------------------------------
+template <typename T> struct H1Store;
+template <> struct H1Store<float> {
+  static __device__ __forceinline__ void store(void* H1, int64_t row, int lane, const float* h) {
+    __nv_bfloat162 p[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) p[q] = __floats2bfloat162_rn(h[2 * q], h[2 * q + 1]);
+    reinterpret_cast<uint4*>((__nv_bfloat16*)H1 + row * HID)[lane] = *reinterpret_cast<uint4*>(p);
+  }
+};
+template <> struct H1Store<double> {
+  static __device__ __forceinline__ void store(void* H1, int64_t row, int lane, const double* h) {
+    double* d = (double*)H1 + row * HID + lane * 8;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) d[q] = h[q];
+  }
+};
+template <typename T> __device__ __forceinline__ T gelu_t(T x);
+template <> __device__ __forceinline__ float gelu_t<float>(float x) { return gelu_f(x); }
+template <> __device__ __forceinline__ double gelu_t<double>(double x) { return gelu_d(x); }
+
+// Sweep prep for edge e of sweep s: proposal, proposed occupation, moves, h1.
+template <typename T>
+__global__ void k_prep_sweep(int64_t B, int N, const uint64_t* __restrict__ occ, const int32_t* __restrict__ edges,
+                             int e, int s_local, int E, float hop_rate, uint64_t seed, uint64_t sweep_idx,
+                             const float* __restrict__ rm, const uint8_t* __restrict__ rb,
+                             const float* __restrict__ ra, const T* __restrict__ z0, const T* __restrict__ w0t,
+                             uint64_t* __restrict__ prop_occ, PropRec* __restrict__ rec, void* __restrict__ H1) {
+  const int lane = threadIdx.x & 31;
+  const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (w >= B) return;
+  uint64_t up = occ[2 * w], dn = occ[2 * w + 1];
+  const int i = edges[2 * e], j = edges[2 * e + 1];
+  const int xi = site_state(up, dn, i), xj = site_state(up, dn, j);
+  PropRec r{0, 0, 0, 0.f};
+  int a[2] = {0, 0}, b[2] = {0, 0};
+  if (xi != xj) {
+    float u_move, u_acc;
+    int bit;
+    if (rm) {
+      size_t ridx = ((size_t)s_local * E + e) * (size_t)B + (size_t)w;
+      u_move = rm[ridx]; bit = rb[ridx] & 1; u_acc = ra[ridx];
+    } else {
+      EdgeDraw d = draw_edge(seed, (uint64_t)w, sweep_idx, (uint32_t)e);
+      u_move = d.u_move; bit = d.bit; u_acc = d.u_acc;
+    }
+    int ni, nj;
+    propose_pair(xi, xj, u_move, bit, hop_rate, ni, nj);
+    Moves mv = pair_moves(i, j, xi, ni, N);
+    for (int q = 0; q < mv.n; ++q) { a[q] = mv.a[q]; b[q] = mv.b[q]; apply_move(up, dn, N, a[q], b[q]); }
+    r.flag = 1;
+    r.nmov = mv.n;
+    r.moves = a[0] | (b[0] << 8) | (a[1] << 16) | (b[1] << 24);
+    r.u_acc = u_acc;
+  }
+  if (lane == 0) {
+    prop_occ[2 * w] = up;
+    prop_occ[2 * w + 1] = dn;
+    rec[w] = r;
+  }
+  if (!r.flag) return;
+  T h[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) h[q] = z0[w * HID + lane * 8 + q];
+  for (int m = 0; m < r.nmov; ++m) {
+#pragma unroll
+    for (int q = 0; q < 8; ++q) h[q] += w0t[b[m] * HID + lane * 8 + q] - w0t[a[m] * HID + lane * 8 + q];
+  }
+#pragma unroll
+  for (int q = 0; q < 8; ++q) h[q] = gelu_t<T>(h[q]);
+  H1Store<T>::store(H1, w, lane, h);
+}
+
+// z0 = b0 + sum of W0 columns of the occupied orbitals (from scratch); h1 -> H1.
+template <typename T>
+__global__ void k_prep_fresh(int64_t R, int N, const uint64_t* __restrict__ occ, const T* __restrict__ w0t,
+                             const T* __restrict__ b0, T* __restrict__ z0_out, void* __restrict__ H1) {
+  const int lane = threadIdx.x & 31;
+  const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (w >= R) return;
+  const uint64_t up = occ[2 * w], dn = occ[2 * w + 1];
+  T h[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) h[q] = b0[lane * 8 + q];
+  for (int sp = 0; sp < 2; ++sp) {
+    uint64_t m = sp ? dn : up;
+    while (m) {
+      const int site = __ffsll((long long)m) - 1;
+      m &= m - 1;
+      const int o = sp * N + site;
+#pragma unroll
+      for (int q = 0; q < 8; ++q) h[q] += w0t[o * HID + lane * 8 + q];
+    }
+  }
+  if (z0_out) {
+#pragma unroll
+    for (int q = 0; q < 8; ++q) z0_out[w * HID + lane * 8 + q] = h[q];
+  }
+#pragma unroll
+  for (int q = 0; q < 8; ++q) h[q] = gelu_t<T>(h[q]);
+  H1Store<T>::store(H1, w, lane, h);
+}
+
+// Local-energy prep: pair p = (walker, hop term) -> connected configuration
+// occupation, coefficient, z0 + W0 column difference, h1.
+template <typename T>
+__global__ void k_prep_conn(int64_t P, int N, const int32_t* __restrict__ pairs /*(P,2) walker, term*/,
+                            const uint64_t* __restrict__ occ, const int32_t* __restrict__ edges, double t,
+                            const T* __restrict__ z0, const T* __restrict__ w0t, uint64_t* __restrict__ row_occ,
+                            double* __restrict__ coeff, void* __restrict__ H1) {
+  const int lane = threadIdx.x & 31;
+  const int64_t p = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (p >= P) return;
+  const int w = pairs[2 * p], term = pairs[2 * p + 1];
+  const uint64_t up = occ[2 * (int64_t)w], dn = occ[2 * (int64_t)w + 1];
+  const int e = term >> 1, s = (term & 1) ? 0 : 1;
+  int i = edges[2 * e], j = edges[2 * e + 1];
+  if (i > j) { int tt = i; i = j; j = tt; }
+  const uint64_t m = s ? up : dn;
+  const int oi = (int)((m >> i) & 1ull);
+  const int base = s ? 0 : N;
+  const int a = base + (oi ? i : j), b = base + (oi ? j : i);
+  uint64_t eu = up, ed = dn;
+  apply_move(eu, ed, N, a, b);
+  if (lane == 0) {
+    row_occ[2 * p] = eu;
+    row_occ[2 * p + 1] = ed;
+    coeff[p] = symmray_parity(up, dn, i, j, s) ? t : -t;
+  }
+  T h[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q)
+    h[q] = gelu_t<T>(z0[(int64_t)w * HID + lane * 8 + q] + w0t[b * HID + lane * 8 + q] - w0t[a * HID + lane * 8 + q]);
+  H1Store<T>::store(H1, p, lane, h);
+}
+
+// ---------------------------------------------------------------------------
+// tcgen05 GEMM: D[128 x 256] = A[128 x 256] * B[256 x 256]^T, both K-major bf16
+// in SWIZZLE_128B smem loaded by TMA; D in TMEM; fused epilogues.
+// ---------------------------------------------------------------------------
+enum { EPI_GELU_BF16 = 0, EPI_BACKFLOW = 1 };
+
+struct EpiArgs {
+  // EPI_GELU_BF16
+  const float* bias;          // (256)
+  __nv_bfloat16* out;         // (rows, 256)
+  // EPI_BACKFLOW
+  const uint64_t* row_occ;    // (rows, 2)
+  const float* mbase;         // (n_orb, nf)
+  const float* outb;          // (n_orb * nf)
+  float* Aout;                // (rows, nf, nf)
+  float scale;
+  int n_sites, nf;
+};
+
+template <int EPI>
+__global__ void __launch_bounds__(128, 1)
+    k_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int rows, EpiArgs ea,
+              int* __restrict__ err) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* sm = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint8_t* sA = sm;
+  uint8_t* sB = sm + SMEM_A;
+  uint64_t* bars = (uint64_t*)(sm + SMEM_A + SMEM_B);
+  uint32_t* tslot = (uint32_t*)(bars + 2);
+  int* sflag = (int*)(bars + 3);
+  float* sc0 = (float*)(sm + SMEM_A + SMEM_B + 64);   // bias, or M_base slice
+  float* sc1 = sc0 + TN;                               // out_b slice
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int row0 = blockIdx.x * TM;
+  const int brow0 = blockIdx.y * TN;
+  if (threadIdx.x == 0) {
+    tc::mbar_init(&bars[0], 1);
+    tc::mbar_init(&bars[1], 1);
+    tc::fence_mbar_init();
+    tc::prefetch_tmap(&tmA);
+    tc::prefetch_tmap(&tmB);
+    *sflag = 1;
+  }
+  if (EPI == EPI_GELU_BF16) {
+    for (int q = threadIdx.x; q < TN; q += blockDim.x) sc0[q] = ea.bias[brow0 + q];
+  } else {
+    for (int q = threadIdx.x; q < TN; q += blockDim.x) {
+      sc0[q] = ea.mbase[brow0 + q];
+      sc1[q] = ea.outb[brow0 + q];
+    }
+  }
+  if (warp == 0) tc::tmem_alloc(tslot, 256);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tbase = *tslot;
+  if (threadIdx.x == 0) {
+    tc::mbar_arrive_expect_tx(&bars[0], SMEM_A + SMEM_B);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) tc::tma_load_2d(sA + j * (TM * 128), &tmA, &bars[0], j * 64, row0);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) tc::tma_load_2d(sB + j * (TN * 128), &tmB, &bars[0], j * 64, brow0);
+    if (tc::mbar_wait(&bars[0], 0)) {
+      tc::fence_after_sync();
+      constexpr uint32_t idesc = tc::idesc_bf16_f32(TM, TN);
+#pragma unroll
+      for (int ks = 0; ks < HID / 16; ++ks) {
+        const int j = ks >> 2, kk = ks & 3;
+        const uint64_t ad = tc::sdesc_sw128(tc::smem_u32(sA + j * (TM * 128)) + kk * 32);
+        const uint64_t bd = tc::sdesc_sw128(tc::smem_u32(sB + j * (TN * 128)) + kk * 32);
+        tc::mma_bf16(tbase, ad, bd, idesc, ks > 0 ? 1u : 0u);
+      }
+      tc::mma_commit(&bars[1]);
+    } else {
+      *sflag = 0;
+      atomicExch(err, VMC_ERR_TIMEOUT);
+    }
+  }
+  __syncthreads();
+  if (*sflag) {
+    const bool done = tc::mbar_wait(&bars[1], 0);
+    tc::fence_after_sync();
+    if (!done) {
+      if (lane == 0) atomicExch(err, VMC_ERR_TIMEOUT);
+    } else {
+      const int r = warp * 32 + lane;
+      const int64_t row = (int64_t)row0 + r;
+      const bool live = row < rows;
+      uint64_t up = 0, dn = 0;
+      if (EPI == EPI_BACKFLOW && live) { up = ea.row_occ[2 * row]; dn = ea.row_occ[2 * row + 1]; }
+#pragma unroll 1
+      for (int cc = 0; cc < TN / 32; ++cc) {
+        float v[32];
+        tc::tmem_ld32(tbase + ((uint32_t)(warp * 32) << 16) + (uint32_t)(cc * 32), v);
+        if (!live) continue;
+        if (EPI == EPI_GELU_BF16) {
+          const int n0 = brow0 + cc * 32;
+          uint32_t pk[16];
+#pragma unroll
+          for (int q = 0; q < 16; ++q) {
+            __nv_bfloat162 h2 = __floats2bfloat162_rn(gelu_f(v[2 * q] + sc0[cc * 32 + 2 * q]),
+                                                      gelu_f(v[2 * q + 1] + sc0[cc * 32 + 2 * q + 1]));
+            pk[q] = *reinterpret_cast<uint32_t*>(&h2);
+          }
+          uint4* dst = reinterpret_cast<uint4*>(ea.out + row * HID + n0);
+#pragma unroll
+          for (int q = 0; q < 4; ++q) dst[q] = make_uint4(pk[4 * q], pk[4 * q + 1], pk[4 * q + 2], pk[4 * q + 3]);
+        } else {
+          const int nf = ea.nf;
+          const int col = brow0 + cc * 32;          // flat output index = orbital * nf + c
+          const int orb = col / nf, c0 = col - orb * nf;
+          const int N = ea.n_sites;
+          if (!orb_occupied(up, dn, N, orb)) continue;
+          const int pos = orb_prefix(up, dn, N, orb);
+          if (pos >= nf) continue;
+          float* dst = ea.Aout + ((size_t)row * nf + pos) * nf + c0;
+          const float* mb = sc0 + cc * 32;   // == M_base[orb][c0 ..], staged
+          const float* ob = sc1 + cc * 32;   // == out_b[orb * nf + c0 ..], staged
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            float4 o;
+            o.x = mb[4 * q + 0] + ea.scale * (v[4 * q + 0] + ob[4 * q + 0]);
+            o.y = mb[4 * q + 1] + ea.scale * (v[4 * q + 1] + ob[4 * q + 1]);
+            o.z = mb[4 * q + 2] + ea.scale * (v[4 * q + 2] + ob[4 * q + 2]);
+            o.w = mb[4 * q + 3] + ea.scale * (v[4 * q + 3] + ob[4 * q + 3]);
+            reinterpret_cast<float4*>(dst)[q] = o;
+          }
+        }
+      }
+    }
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tbase, 256);
+}
+
+// ---------------------------------------------------------------------------
+// Persistent backflow GEMM: one CTA per SM walks a contiguous range of work
+// items (orbital group g, walker tile t) in g-major order.  The out_w rows of
+// group g (256 x 256 bf16, 128 KB) stay resident in shared memory while the
+// hidden-activation tiles (128 x 256 bf16) stream through a 4-stage pipeline
+// (one stage per 64-wide K atom).  Warp roles: warp 0 = TMA producer, warp 1 =
+// MMA issuer (one thread), warps 2..5 = epilogue (TMEM lane quadrants 2,3,0,1).
+// Two TMEM accumulators (2 x 256 columns) let the epilogue of item i overlap
+// the MMAs of item i+1.
+// ---------------------------------------------------------------------------
+constexpr int PB_THREADS = 192;
+constexpr int PB_SMEM = SMEM_A + SMEM_B + 1024 + 256 + 2 * TN * 4;
+
+struct PBArgs {
+  const uint64_t* row_occ;  // (R, 2)
+  const float* mbase;       // (n_orb * nf) flat
+  const float* outb;        // (n_orb * nf)
+  float* Aout;              // (R, nf, nf)
+  float scale;
+  int n_sites, nf, R, n_tiles, n_items;
+};
+
+__global__ void __launch_bounds__(PB_THREADS, 1)
+    k_backflow_persistent(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, PBArgs pa,
+                          int* __restrict__ err) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* sm = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint8_t* sA = sm;                 // 4 atoms x 16 KB
+  uint8_t* sB = sm + SMEM_A;        // 4 atoms x 32 KB
+  uint64_t* bar = (uint64_t*)(sm + SMEM_A + SMEM_B);
+  uint64_t* bfull = bar + 0;
+  uint64_t* bempty = bar + 1;
+  uint64_t* afull = bar + 2;    // [4]
+  uint64_t* aempty = bar + 6;   // [4]
+  uint64_t* tfull = bar + 10;   // [2]
+  uint64_t* tempty = bar + 12;  // [2]
+  uint32_t* tslot = (uint32_t*)(bar + 14);
+  volatile int* abort_flag = (volatile int*)(bar + 15);
+  float* cM = (float*)(sm + SMEM_A + SMEM_B + 256);
+  float* cO = cM + TN;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int per = (pa.n_items + gridDim.x - 1) / gridDim.x;
+  const int it0 = blockIdx.x * per;
+  const int it1 = min(pa.n_items, it0 + per);
+  if (threadIdx.x == 0) {
+    tc::mbar_init(bfull, 1);
+    tc::mbar_init(bempty, 1);
+    for (int j = 0; j < 4; ++j) { tc::mbar_init(&afull[j], 1); tc::mbar_init(&aempty[j], 1); }
+    for (int b = 0; b < 2; ++b) { tc::mbar_init(&tfull[b], 1); tc::mbar_init(&tempty[b], 4); }
+    *abort_flag = 0;
+    tc::fence_mbar_init();
+    tc::prefetch_tmap(&tmA);
+    tc::prefetch_tmap(&tmB);
+  }
+  if (warp == 0) tc::tmem_alloc(tslot, 512);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tbase = *tslot;
+  if (it0 < it1) {
+    if (warp == 0) {
+      if (lane == 0) {  // ---------------- TMA producer ----------------
+        int cur_g = -1, ng = 0;
+        for (int it = it0, i = 0; it < it1 && !*abort_flag; ++it, ++i) {
+          const int g = it / pa.n_tiles, t = it - g * pa.n_tiles;
+          if (g != cur_g) {
+            if (cur_g >= 0 && !tc::mbar_wait(bempty, (ng - 1) & 1)) { *abort_flag = 1; atomicExch(err, VMC_ERR_TIMEOUT); break; }
+            tc::mbar_arrive_expect_tx(bfull, SMEM_B);
+            for (int j = 0; j < 4; ++j) tc::tma_load_2d(sB + j * (TN * 128), &tmB, bfull, j * 64, g * TN);
+            cur_g = g;
+            ++ng;
+          }
+          for (int j = 0; j < 4; ++j) {
+            if (i > 0 && !tc::mbar_wait(&aempty[j], (i - 1) & 1)) { *abort_flag = 1; atomicExch(err, VMC_ERR_TIMEOUT); break; }
+            tc::mbar_arrive_expect_tx(&afull[j], TM * 128);
+            tc::tma_load_2d(sA + j * (TM * 128), &tmA, &afull[j], j * 64, t * TM);
+          }
+        }
+      }
+    } else if (warp == 1) {
+      if (lane == 0) {  // ---------------- MMA issuer ----------------
+        constexpr uint32_t idesc = tc::idesc_bf16_f32(TM, TN);
+        int cur_g = -1, ng = 0;
+        for (int it = it0, i = 0; it < it1 && !*abort_flag; ++it, ++i) {
+          const int g = it / pa.n_tiles;
+          if (g != cur_g) {
+            if (!tc::mbar_wait(bfull, ng & 1)) { *abort_flag = 1; atomicExch(err, VMC_ERR_TIMEOUT); break; }
+            cur_g = g;
+            ++ng;
+          }
+          const int buf = i & 1;
+          if (i >= 2 && !tc::mbar_wait(&tempty[buf], ((i >> 1) - 1) & 1)) { *abort_flag = 1; atomicExch(err, VMC_ERR_TIMEOUT); break; }
+          tc::fence_after_sync();
+          const uint32_t dt = tbase + (uint32_t)(buf * TN);
+          bool ok = true;
+          for (int j = 0; j < 4; ++j) {
+            if (!tc::mbar_wait(&afull[j], i & 1)) { ok = false; break; }
+            tc::fence_after_sync();
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk) {
+              const uint64_t ad = tc::sdesc_sw128(tc::smem_u32(sA + j * (TM * 128)) + kk * 32);
+              const uint64_t bd = tc::sdesc_sw128(tc::smem_u32(sB + j * (TN * 128)) + kk * 32);
+              tc::mma_bf16(dt, ad, bd, idesc, (j | kk) ? 1u : 0u);
+            }
+            tc::mma_commit(&aempty[j]);
+          }
+          if (!ok) { *abort_flag = 1; atomicExch(err, VMC_ERR_TIMEOUT); break; }
+          tc::mma_commit(&tfull[buf]);
+          const int gn = (it + 1 < it1) ? (it + 1) / pa.n_tiles : -2;
+          if (gn != g) tc::mma_commit(bempty);  // B of group g no longer needed
+        }
+      }
+    } else {  // ---------------- epilogue warps 2..5 ----------------
+      const int quad = warp & 3;
+      const int et = threadIdx.x - 64;   // 0..127
+      int cur_g = -1;
+      for (int it = it0, i = 0; it < it1; ++it, ++i) {
+        const int g = it / pa.n_tiles, t = it - g * pa.n_tiles;
+        if (g != cur_g) {
+          asm volatile("bar.sync 1, 128;" ::: "memory");
+          for (int q = et; q < TN; q += 128) { cM[q] = pa.mbase[g * TN + q]; cO[q] = pa.outb[g * TN + q]; }
+          asm volatile("bar.sync 1, 128;" ::: "memory");
+          cur_g = g;
+        }
+        const int buf = i & 1;
+        bool ok = tc::mbar_wait(&tfull[buf], (i >> 1) & 1);
+        ok = __all_sync(VMC_FULL_MASK, ok);
+        if (!ok) { if (lane == 0) { *abort_flag = 1; atomicExch(err, VMC_ERR_TIMEOUT); } break; }
+        tc::fence_after_sync();
+        const int64_t row = (int64_t)t * TM + quad * 32 + lane;
+        const bool live = row < pa.R;
+        uint64_t up = 0, dn = 0;
+        if (live) { up = pa.row_occ[2 * row]; dn = pa.row_occ[2 * row + 1]; }
+        const int nf = pa.nf, N = pa.n_sites;
+#pragma unroll 1
+        for (int cc = 0; cc < TN / 32; ++cc) {
+          float v[32];
+          tc::tmem_ld32(tbase + (uint32_t)(buf * TN) + ((uint32_t)(quad * 32) << 16) + (uint32_t)(cc * 32), v);
+          if (!live) continue;
+          const int col = g * TN + cc * 32;
+          const int orb = col / nf, c0 = col - orb * nf;
+          if (!orb_occupied(up, dn, N, orb)) continue;
+          const int pos = orb_prefix(up, dn, N, orb);
+          if (pos >= nf) continue;
+          float* dst = pa.Aout + ((size_t)row * nf + pos) * nf + c0;
+          const float* mb = cM + cc * 32;
+          const float* ob = cO + cc * 32;
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            const float4 m4 = reinterpret_cast<const float4*>(mb)[q];
+            const float4 o4 = reinterpret_cast<const float4*>(ob)[q];
+            float4 o;
+            o.x = m4.x + pa.scale * (v[4 * q + 0] + o4.x);
+            o.y = m4.y + pa.scale * (v[4 * q + 1] + o4.y);
+            o.z = m4.z + pa.scale * (v[4 * q + 2] + o4.z);
+            o.w = m4.w + pa.scale * (v[4 * q + 3] + o4.w);
+            reinterpret_cast<float4*>(dst)[q] = o;
+          }
+        }
+        tc::fence_before_sync();
+        __syncwarp();
+        if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc::smem_u32(&tempty[buf])) : "memory");
+      }
+    }
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tbase, 512);
+}
+
+// ---------------------------------------------------------------------------
+// FP64 twins (CUDA cores): layer 1 and backflow, one block per row
+// ---------------------------------------------------------------------------
+__global__ void k_layer1_f64(int64_t R, const double* __restrict__ H1, const double* __restrict__ W1,
+                             const double* __restrict__ b1, double* __restrict__ H2) {
+  __shared__ double h[HID];
+  const int64_t row = blockIdx.x;
+  h[threadIdx.x] = H1[row * HID + threadIdx.x];
+  __syncthreads();
+  const int n = threadIdx.x;
+  double acc = b1[n];
+  for (int k = 0; k < HID; ++k) acc = fma(W1[(size_t)n * HID + k], h[k], acc);
+  H2[row * HID + n] = gelu_d(acc);
+}
+
+__global__ void k_backflow_f64(int64_t R, int N, int nf, const uint64_t* __restrict__ row_occ,
+                               const double* __restrict__ H2, const double* __restrict__ outw,
+                               const double* __restrict__ outb, const double* __restrict__ mbase, double scale,
+                               double* __restrict__ A) {
+  __shared__ double h[HID];
+  __shared__ int orbs[64];
+  const int64_t row = blockIdx.x;
+  const uint64_t up = row_occ[2 * row], dn = row_occ[2 * row + 1];
+  h[threadIdx.x] = H2[row * HID + threadIdx.x];
+  if (threadIdx.x < 2 * N && orb_occupied(up, dn, N, threadIdx.x)) {
+    int pos = orb_prefix(up, dn, N, threadIdx.x);
+    if (pos < 64) orbs[pos] = threadIdx.x;
+  }
+  __syncthreads();
+  const bool ok = (__popcll(up) + __popcll(dn)) == nf;
+  for (int idx = threadIdx.x; idx < nf * nf; idx += blockDim.x) {
+    const int pos = idx / nf, c = idx - pos * nf;
+    double val = 0.0;
+    if (ok) {
+      const int o = orbs[pos];
+      const double* wr = outw + ((size_t)o * nf + c) * HID;
+      double acc = outb[(size_t)o * nf + c];
+      for (int k = 0; k < HID; ++k) acc = fma(wr[k], h[k], acc);
+      val = mbase[(size_t)o * nf + c] + scale * acc;
+    }
+    A[(size_t)row * nf * nf + idx] = val;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// log|det| + sign, one warp per row
+// ---------------------------------------------------------------------------
+struct Det { double logabs; double sign; };
+
+// FP32 registers, rows lane and lane+32, no physical row swaps: a retired-row
+// mask U tracks the pivots; the permutation parity is accumulated as the
+// number of unretired rows below each pivot.
+//
+// Code-size-aware schedule: the elimination runs in NF/16 phases of 16 steps.
+// Within a phase of width W the live columns of every row are kept at
+// register indices 0..W-1 and rotate by one per step (the shift is fused into
+// the update FMA: a[c-1] = a[c] - f * pivot[c]), so the step body has only
+// compile-time register indices and runs as a runtime loop; each phase is a
+// separate instantiation with W = NF, NF-16, ... (work per step ~ 2 W FMAs
+// instead of the fixed 2 NF).
+template <int NF>
+struct LuRegs {
+  float a[NF / 32][NF];
+  uint64_t U;
+  float mant;
+  int expo, neg;
+  bool ok;
+};
+
+template <int NF, int W>
+__device__ __forceinline__ void lu_phase(LuRegs<NF>& S, float* prow, int lane) {
+  constexpr int R = NF / 32;
+#pragma unroll 1
+  for (int t = 0; t < 16; ++t) {
+    // pivot: max |a| over unretired rows in a single warp reduction on a packed
+    // key (|a| bits with the low 6 mantissa bits replaced by 63 - row: larger
+    // magnitude wins, ties -> smaller row).  The 6 dropped bits only matter for
+    // magnitudes equal to 2^-17 relative, where either choice is a valid pivot.
+    unsigned key = 0;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int row = lane + 32 * r;
+      if ((S.U >> row) & 1ull) {
+        const unsigned kb = (__float_as_uint(fabsf(S.a[r][0])) & ~63u) | (unsigned)(63 - row);
+        key = kb > key ? kb : key;
+      }
+    }
+    key = __reduce_max_sync(VMC_FULL_MASK, key);
+    const int p = 63 - (int)(key & 63u);
+    const float best = __uint_as_float(key & ~63u);
+    // pivot row -> shared memory (warp-uniform branch on the register row)
+    if (R > 1 && (p >> 5)) {
+      if ((p & 31) == lane) {
+#pragma unroll
+        for (int q = 0; q < W / 4; ++q)
+          reinterpret_cast<float4*>(prow)[q] =
+              make_float4(S.a[R - 1][4 * q], S.a[R - 1][4 * q + 1], S.a[R - 1][4 * q + 2], S.a[R - 1][4 * q + 3]);
+      }
+    } else {
+      if ((p & 31) == lane) {
+#pragma unroll
+        for (int q = 0; q < W / 4; ++q)
+          reinterpret_cast<float4*>(prow)[q] =
+              make_float4(S.a[0][4 * q], S.a[0][4 * q + 1], S.a[0][4 * q + 2], S.a[0][4 * q + 3]);
+      }
+    }
+    __syncwarp();
+    float pv = prow[0];
+    const bool pvalid = key != 0u && (best > 0.0f) && isfinite(best);
+    if (!pvalid) { S.ok = false; pv = 1.0f; }
+    S.neg ^= (pv < 0.0f);
+    S.neg ^= __popcll(S.U & ((1ull << p) - 1ull)) & 1;
+    S.U &= ~(1ull << p);
+    // |det| as mantissa in [1, 2) times 2^expo (normal floats; pivots are
+    // O(1e-3..1e1) here, far from the FP32 limits)
+    const float m = S.mant * fabsf(pv);
+    const unsigned mb = __float_as_uint(m);
+    S.expo += (int)((mb >> 23) & 255u) - 127;
+    S.mant = __uint_as_float((mb & 0x007FFFFFu) | 0x3F800000u);
+    const float ipv = __frcp_rn(pv);
+    float pr[W];
+#pragma unroll
+    for (int q = 0; q < W / 4; ++q) {
+      const float4 t4 = reinterpret_cast<const float4*>(prow)[q];
+      pr[4 * q] = t4.x; pr[4 * q + 1] = t4.y; pr[4 * q + 2] = t4.z; pr[4 * q + 3] = t4.w;
+    }
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const float f = S.a[r][0] * ipv;   // retired rows keep updating harmlessly
+#pragma unroll
+      for (int c = 1; c < W; ++c) S.a[r][c - 1] = fmaf(-f, pr[c], S.a[r][c]);
+    }
+    __syncwarp();
+  }
+}
+
+template <int NF>
+__device__ __forceinline__ Det warp_logdet_f32(const float* __restrict__ A, float* prow) {
+  static_assert(NF == 32 || NF == 64, "NF must be 32 or 64");
+  constexpr int R = NF / 32;
+  const int lane = threadIdx.x & 31;
+  LuRegs<NF> S;
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const float4* src = reinterpret_cast<const float4*>(A + (size_t)(lane + 32 * r) * NF);
+#pragma unroll
+    for (int q = 0; q < NF / 4; ++q) {
+      float4 t = src[q];
+      S.a[r][4 * q] = t.x; S.a[r][4 * q + 1] = t.y; S.a[r][4 * q + 2] = t.z; S.a[r][4 * q + 3] = t.w;
+    }
+  }
+  S.U = (NF == 64) ? ~0ull : ((1ull << NF) - 1ull);
+  S.mant = 1.0f;
+  S.expo = 0;
+  S.neg = 0;
+  S.ok = true;
+  lu_phase<NF, NF>(S, prow, lane);
+  lu_phase<NF, NF - 16>(S, prow, lane);
+  if constexpr (NF == 64) {
+    lu_phase<NF, 32>(S, prow, lane);
+    lu_phase<NF, 16>(S, prow, lane);
+  }
+  Det d;
+  if (S.ok) {
+    // mantissa in [1, 2): FP32 log is accurate to ~1e-7 absolute; the exponent
+    // part is exact; only the final sum is FP64 (FP64 pipes are scarce on GB300)
+    d.logabs = (double)logf(S.mant) + (double)S.expo * 0.69314718055994530942;
+    d.sign = S.neg ? -1.0 : 1.0;
+  } else {
+    d.logabs = -INFINITY;
+    d.sign = 0.0;
+  }
+  return d;
+}
+
+// FP64 in shared memory (nf <= 64 at run time), same retired-row scheme.
+__device__ Det warp_logdet_f64(const double* __restrict__ A, int nf, double* s /*nf*(nf+1)*/) {
+  const int lane = threadIdx.x & 31;
+  const int ld = nf + 1;
+  for (int idx = lane; idx < nf * nf; idx += 32) s[(idx / nf) * ld + idx % nf] = A[idx];
+  __syncwarp();
+  uint64_t U = (nf == 64) ? ~0ull : ((1ull << nf) - 1ull);
+  double la = 0.0;
+  int neg = 0;
+  bool ok = true;
+  for (int k = 0; k < nf; ++k) {
+    double best = -1.0;
+    int bi = 1 << 30;
+    for (int r = lane; r < nf; r += 32) {
+      if ((U >> r) & 1ull) {
+        const double v = fabs(s[r * ld + k]);
+        if (v > best) { best = v; bi = r; }
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const double ob = __shfl_xor_sync(VMC_FULL_MASK, best, o);
+      const int oi = __shfl_xor_sync(VMC_FULL_MASK, bi, o);
+      if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+    }
+    const int p = bi;
+    if (p >= nf) { ok = false; break; }  // no finite pivot candidate (warp-uniform)
+    double pv = s[p * ld + k];
+    if (!(best > 0.0) || !isfinite(best)) { ok = false; pv = 1.0; }
+    neg ^= (pv < 0.0);
+    neg ^= __popcll(U & ((1ull << p) - 1ull)) & 1;
+    U &= ~(1ull << p);
+    la += log(fabs(pv));
+    __syncwarp();
+    for (int r = lane; r < nf; r += 32) {
+      if ((U >> r) & 1ull) {
+        const double f = s[r * ld + k] / pv;
+        for (int c = k + 1; c < nf; ++c) s[r * ld + c] -= f * s[p * ld + c];
+      }
+    }
+    __syncwarp();
+  }
+  Det d;
+  d.logabs = ok ? la : -INFINITY;
+  d.sign = ok ? (neg ? -1.0 : 1.0) : 0.0;
+  return d;
+}
+
+enum { LD_ACCEPT = 0, LD_EVAL = 1, LD_ELOC = 2 };
+
+struct LdArgs {
+  // accept
+  const PropRec* rec;
+  const uint64_t* prop_occ;
+  uint64_t* occ;
+  int32_t* nacc;
+  void* z0;            // float or double (B, HID)
+  const void* w0t;
+  // accept / eval
+  double* sign;
+  double* logabs;
+  // eloc
+  const int32_t* pairs;
+  const double* coeff;
+  double* term;
+};
+
+template <typename T, int NF, int MODE>
+__global__ void k_logdet(int64_t R, int64_t row0, int nf, const T* __restrict__ A, LdArgs la) {
+  extern __shared__ __align__(16) uint8_t lsm[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t local = (int64_t)blockIdx.x * (blockDim.x >> 5) + warp;
+  if (local >= R) return;
+  const int64_t row = row0 + local;
+  if (MODE == LD_ACCEPT) {
+    if (!la.rec[row].flag) return;
+  }
+  Det d;
+  if constexpr (sizeof(T) == 4) {
+    float* prow = reinterpret_cast<float*>(lsm) + warp * 64;
+    d = warp_logdet_f32<NF>(reinterpret_cast<const float*>(A) + (size_t)local * NF * NF, prow);
+  } else {
+    double* s = reinterpret_cast<double*>(lsm) + (size_t)warp * (64 * 65);
+    d = warp_logdet_f64(reinterpret_cast<const double*>(A) + (size_t)local * nf * nf, nf, s);
+  }
+  if (MODE == LD_EVAL) {
+    if (lane == 0) { la.sign[row] = d.sign; la.logabs[row] = d.logabs; }
+  } else if (MODE == LD_ELOC) {
+    if (lane == 0) {
+      const int w = la.pairs[2 * row];
+      double v = 0.0;
+      if (d.sign != 0.0 && la.sign[w] != 0.0) v = la.coeff[row] * d.sign * la.sign[w] * exp(d.logabs - la.logabs[w]);
+      la.term[row] = v;
+    }
+  } else {
+    const PropRec r = la.rec[row];
+    // |psi'|^2/|psi|^2 from the FP64 log difference, exponentiated in FP32
+    // (FP32 relative accuracy is ample for comparing against a 24-bit uniform)
+    const float dl2 = (float)(2.0 * (d.logabs - la.logabs[row]));
+    const float prob = expf(fminf(dl2, 80.0f));
+    const bool acc = (d.sign != 0.0) && (r.u_acc < prob);
+    if (!acc) return;
+    if (lane == 0) {
+      la.occ[2 * row] = la.prop_occ[2 * row];
+      la.occ[2 * row + 1] = la.prop_occ[2 * row + 1];
+      la.sign[row] = d.sign;
+      la.logabs[row] = d.logabs;
+      la.nacc[row] += 1;
+    }
+    int a[2], b[2];
+    unpack_moves(r, a, b);
+    T* z0 = reinterpret_cast<T*>(la.z0);
+    const T* w0t = reinterpret_cast<const T*>(la.w0t);
+    for (int m = 0; m < r.nmov; ++m) {
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int u = lane * 8 + q;
+        z0[row * HID + u] += w0t[b[m] * HID + u] - w0t[a[m] * HID + u];
+      }
+    }
+  }
+}
+
+// per-walker local energy: U * doublons + segmented sum of the hop terms
+__global__ void k_eloc_reduce(int64_t B, const uint64_t* __restrict__ occ, const int32_t* __restrict__ offs,
+                              const double* __restrict__ term, double U, double* __restrict__ eloc) {
+  const int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= B) return;
+  double s = U * (double)__popcll(occ[2 * w] & occ[2 * w + 1]);
+  for (int q = offs[w]; q < offs[w + 1]; ++q) s += term[q];
+  eloc[w] = s;
+}
+
+// number of valid hop terms per walker (T = 2E hop slots)
+__global__ void k_count_hops(int64_t B, int N, const uint64_t* __restrict__ occ, const int32_t* __restrict__ edges,
+                             int E, int32_t* __restrict__ cnt) {
+  const int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= B) return;
+  const uint64_t up = occ[2 * w], dn = occ[2 * w + 1];
+  int c = 0;
+  for (int e = 0; e < E; ++e) {
+    const int i = edges[2 * e], j = edges[2 * e + 1];
+    c += (int)(((up >> i) ^ (up >> j)) & 1ull) + (int)(((dn >> i) ^ (dn >> j)) & 1ull);
+  }
+  cnt[w] = c;
+}
+
+__global__ void k_fill_pairs(int64_t B, int N, const uint64_t* __restrict__ occ, const int32_t* __restrict__ edges,
+                             int E, const int32_t* __restrict__ offs, int32_t* __restrict__ pairs) {
+  const int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= B) return;
+  const uint64_t up = occ[2 * w], dn = occ[2 * w + 1];
+  int q = offs[w];
+  for (int e = 0; e < E; ++e) {
+    const int i = edges[2 * e], j = edges[2 * e + 1];
+    if (((up >> i) ^ (up >> j)) & 1ull) { pairs[2 * q] = (int)w; pairs[2 * q + 1] = 2 * e; ++q; }
+    if (((dn >> i) ^ (dn >> j)) & 1ull) { pairs[2 * q] = (int)w; pairs[2 * q + 1] = 2 * e + 1; ++q; }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host helpers
+// ---------------------------------------------------------------------------
+PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+
+bool get_encoder() {
+  if (g_encode) return true;
+  void* fn = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+      q != cudaDriverEntryPointSuccess || !fn)
+    return false;
+  g_encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+  return true;
+}
+
+// bf16 row-major (rows x 256) tensor map, box {64, box_rows}, SWIZZLE_128B
+bool tmap_bf16(CUtensorMap* m, const void* base, uint64_t rows, uint32_t box_rows) {
+  if (!get_encoder()) return false;
+  if (((uintptr_t)base & 15) != 0) return false;
+  cuuint64_t gdim[2] = {(cuuint64_t)HID, (cuuint64_t)rows};
+  cuuint64_t gstr[1] = {(cuuint64_t)HID * 2};
+  cuuint32_t box[2] = {64, box_rows};
+  cuuint32_t es[2] = {1, 1};
+  CUresult r = g_encode(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), gdim, gstr, box, es,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+struct NetF32 {
+  const float* w0t;             // (n_orb, 256)
+  const float* b0;              // (256)
+  const __nv_bfloat16* w1;      // (256, 256) bf16
+  const float* b1;              // (256)
+  const __nv_bfloat16* outw;    // (n_orb*nf, 256) bf16
+  const float* outb;            // (n_orb*nf)
+  const float* mbase;           // (n_orb, nf)
+};
+struct NetF64 {
+  const double* w0t; const double* b0; const double* w1; const double* b1; const double* outw; const double* outb;
+  const double* mbase;
+};
+
+// Workspace for R rows: H1, H2 (bf16 or fp64, R x 256), A (R x nf x nf).
+struct Work {
+  void* H1; void* H2; void* A;
+};
+
+// Rows per backflow+LU chunk: 4096 x 64 x 64 FP32 orbital matrices = 64 MB,
+// small enough to stay resident in L2 between the GEMM epilogue and the LU.
+constexpr int64_t kChunkRows = 4096;
+
+int g_num_sms = 0;
+int num_sms() {
+  if (!g_num_sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (g_num_sms <= 0) g_num_sms = 148;
+  }
+  return g_num_sms;
+}
+
+void set_attrs();
+
+int launch_eval_rows(int prec, int64_t R, int N, int nf, const uint64_t* row_occ, const void* net, double scale,
+                     const Work& wk, int* err, cudaStream_t st, int ldmode, const LdArgs& la) {
+  const int n_orb = 2 * N;
+  if (prec == 0) {
+    const NetF32& n = *(const NetF32*)net;
+    CUtensorMap tH1, tW1, tOW;
+    if (!tmap_bf16(&tH1, wk.H1, (uint64_t)R, TM) || !tmap_bf16(&tW1, n.w1, HID, TN) ||
+        !tmap_bf16(&tOW, n.outw, (uint64_t)n_orb * nf, TN))
+      return VMC_ERR_UNSUPPORTED;
+    EpiArgs e1{};
+    e1.bias = n.b1;
+    e1.out = (__nv_bfloat16*)wk.H2;
+    dim3 g1((unsigned)((R + TM - 1) / TM), 1);
+    k_gemm_tc<EPI_GELU_BF16><<<g1, 128, GEMM_SMEM, st>>>(tH1, tW1, (int)R, e1, err);
+    const int n_groups = (n_orb * nf) / TN;
+    const int64_t CH = R < kChunkRows ? R : kChunkRows;
+    const int wpb = 4;
+    const size_t lsmem = wpb * 64 * sizeof(float);
+    for (int64_t c0 = 0; c0 < R; c0 += CH) {
+      const int64_t Rc = (R - c0) < CH ? (R - c0) : CH;
+      CUtensorMap tH2c;
+      if (!tmap_bf16(&tH2c, (const __nv_bfloat16*)wk.H2 + c0 * HID, (uint64_t)Rc, TM)) return VMC_ERR_UNSUPPORTED;
+      PBArgs pa{};
+      pa.row_occ = row_occ + 2 * c0; pa.mbase = n.mbase; pa.outb = n.outb; pa.Aout = (float*)wk.A;
+      pa.scale = (float)scale; pa.n_sites = N; pa.nf = nf; pa.R = (int)Rc;
+      pa.n_tiles = (int)((Rc + TM - 1) / TM);
+      pa.n_items = n_groups * pa.n_tiles;
+      const int grid = pa.n_items < num_sms() ? pa.n_items : num_sms();
+      k_backflow_persistent<<<grid, PB_THREADS, PB_SMEM, st>>>(tH2c, tOW, pa, err);
+      const unsigned gl = (unsigned)((Rc + wpb - 1) / wpb);
+      if (nf == 64) {
+        if (ldmode == LD_ACCEPT) k_logdet<float, 64, LD_ACCEPT><<<gl, 32 * wpb, lsmem, st>>>(Rc, c0, nf, (const float*)wk.A, la);
+        else if (ldmode == LD_EVAL) k_logdet<float, 64, LD_EVAL><<<gl, 32 * wpb, lsmem, st>>>(Rc, c0, nf, (const float*)wk.A, la);
+        else k_logdet<float, 64, LD_ELOC><<<gl, 32 * wpb, lsmem, st>>>(Rc, c0, nf, (const float*)wk.A, la);
+      } else {
+        if (ldmode == LD_ACCEPT) k_logdet<float, 32, LD_ACCEPT><<<gl, 32 * wpb, lsmem, st>>>(Rc, c0, nf, (const float*)wk.A, la);
+        else if (ldmode == LD_EVAL) k_logdet<float, 32, LD_EVAL><<<gl, 32 * wpb, lsmem, st>>>(Rc, c0, nf, (const float*)wk.A, la);
+        else k_logdet<float, 32, LD_ELOC><<<gl, 32 * wpb, lsmem, st>>>(Rc, c0, nf, (const float*)wk.A, la);
+      }
+    }
+  } else {
+    const NetF64& n = *(const NetF64*)net;
+    k_layer1_f64<<<(unsigned)R, HID, 0, st>>>(R, (const double*)wk.H1, n.w1, n.b1, (double*)wk.H2);
+    k_backflow_f64<<<(unsigned)R, 256, 0, st>>>(R, N, nf, row_occ, (const double*)wk.H2, n.outw, n.outb, n.mbase,
+                                                scale, (double*)wk.A);
+    const int wpb = 2;
+    const unsigned gl = (unsigned)((R + wpb - 1) / wpb);
+    const size_t smem = (size_t)wpb * 64 * 65 * sizeof(double);
+    if (ldmode == LD_ACCEPT) {
+      cudaFuncSetAttribute(k_logdet<double, 64, LD_ACCEPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      k_logdet<double, 64, LD_ACCEPT><<<gl, 32 * wpb, smem, st>>>(R, 0, nf, (const double*)wk.A, la);
+    } else if (ldmode == LD_EVAL) {
+      cudaFuncSetAttribute(k_logdet<double, 64, LD_EVAL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      k_logdet<double, 64, LD_EVAL><<<gl, 32 * wpb, smem, st>>>(R, 0, nf, (const double*)wk.A, la);
+    } else {
+      cudaFuncSetAttribute(k_logdet<double, 64, LD_ELOC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      k_logdet<double, 64, LD_ELOC><<<gl, 32 * wpb, smem, st>>>(R, 0, nf, (const double*)wk.A, la);
+    }
+  }
+  VMC_CUDA_CHECK_LAUNCH();
+  return VMC_OK;
+}
+
+bool g_attr_done = false;
+void set_attrs() {
+  if (g_attr_done) return;
+  cudaFuncSetAttribute(k_gemm_tc<EPI_GELU_BF16>, cudaFuncAttributeMaxDynamicSharedMemorySize, GEMM_SMEM);
+  cudaFuncSetAttribute(k_gemm_tc<EPI_BACKFLOW>, cudaFuncAttributeMaxDynamicSharedMemorySize, GEMM_SMEM);
+  cudaFuncSetAttribute(k_backflow_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize, PB_SMEM);
+  g_attr_done = true;
+}
+
+int check_shape(int prec, int N, int nf, int hidden) {
+  if (N < 1 || N > 64 || hidden != HID || nf < 1 || nf > 64) return VMC_ERR_ARGS;
+  if (prec == 0 && ((nf != 32 && nf != 64) || ((2 * N * nf) % TN) != 0)) return VMC_ERR_UNSUPPORTED;
+  if (prec != 0 && prec != 1) return VMC_ERR_ARGS;
+  return VMC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+// net: pointer array, see include/vmc_gb300.h (vmc_nnbf_* documentation)
+int vmc_nnbf_eval(int prec, const void* const* net_ptrs, int n_sites, int nf, int hidden, double bf_scale,
+                  const uint64_t* occ, int64_t R, void* z0_out, void* H1, void* H2, void* A, double* sign,
+                  double* logabs, int* d_err, void* stream) {
+  int st0 = check_shape(prec, n_sites, nf, hidden);
+  if (st0) return st0;
+  if (R < 0 || !net_ptrs || !occ || !H1 || !H2 || !A || !sign || !logabs || !d_err) return VMC_ERR_ARGS;
+  if (R == 0) return VMC_OK;
+  set_attrs();
+  cudaStream_t st = (cudaStream_t)stream;
+  const unsigned gw = (unsigned)((R * 32 + 255) / 256);
+  NetF32 nf32; NetF64 nf64;
+  const void* net;
+  if (prec == 0) {
+    nf32 = NetF32{(const float*)net_ptrs[0], (const float*)net_ptrs[1], (const __nv_bfloat16*)net_ptrs[2],
+                  (const float*)net_ptrs[3], (const __nv_bfloat16*)net_ptrs[4], (const float*)net_ptrs[5],
+                  (const float*)net_ptrs[6]};
+    k_prep_fresh<float><<<gw, 256, 0, st>>>(R, n_sites, occ, nf32.w0t, nf32.b0, (float*)z0_out, H1);
+    net = &nf32;
+  } else {
+    nf64 = NetF64{(const double*)net_ptrs[0], (const double*)net_ptrs[1], (const double*)net_ptrs[2],
+                  (const double*)net_ptrs[3], (const double*)net_ptrs[4], (const double*)net_ptrs[5],
+                  (const double*)net_ptrs[6]};
+    k_prep_fresh<double><<<gw, 256, 0, st>>>(R, n_sites, occ, nf64.w0t, nf64.b0, (double*)z0_out, H1);
+    net = &nf64;
+  }
+  VMC_CUDA_CHECK_LAUNCH();
+  LdArgs la{};
+  la.sign = sign;
+  la.logabs = logabs;
+  return launch_eval_rows(prec, R, n_sites, nf, occ, net, bf_scale, Work{H1, H2, A}, d_err, st, LD_EVAL, la);
+}
+
+int vmc_nnbf_sweep(int prec, const void* const* net_ptrs, int n_sites, int nf, int hidden, double bf_scale,
+                   uint64_t* occ, int64_t B, const int32_t* edges, int n_edges, int n_sweeps, float hopping_rate,
+                   uint64_t seed, uint64_t sweep_offset, const float* r_move, const uint8_t* r_bit, const float* r_acc,
+                   void* z0, double* sign, double* logabs, int32_t* n_acc, uint64_t* prop_occ, void* rec, void* H1,
+                   void* H2, void* A, int* d_err, void* stream) {
+  int st0 = check_shape(prec, n_sites, nf, hidden);
+  if (st0) return st0;
+  if (B < 0 || n_edges < 0 || n_sweeps < 0) return VMC_ERR_ARGS;
+  if ((r_move != nullptr) != (r_acc != nullptr) || (r_move != nullptr) != (r_bit != nullptr)) return VMC_ERR_ARGS;
+  if (B == 0 || n_edges == 0 || n_sweeps == 0) return VMC_OK;
+  if (!net_ptrs || !occ || !edges || !z0 || !sign || !logabs || !n_acc || !prop_occ || !rec || !H1 || !H2 || !A ||
+      !d_err)
+    return VMC_ERR_ARGS;
+  set_attrs();
+  cudaStream_t st = (cudaStream_t)stream;
+  const unsigned gw = (unsigned)((B * 32 + 255) / 256);
+  NetF32 nf32; NetF64 nf64;
+  const void* net;
+  if (prec == 0) {
+    nf32 = NetF32{(const float*)net_ptrs[0], (const float*)net_ptrs[1], (const __nv_bfloat16*)net_ptrs[2],
+                  (const float*)net_ptrs[3], (const __nv_bfloat16*)net_ptrs[4], (const float*)net_ptrs[5],
+                  (const float*)net_ptrs[6]};
+    net = &nf32;
+  } else {
+    nf64 = NetF64{(const double*)net_ptrs[0], (const double*)net_ptrs[1], (const double*)net_ptrs[2],
+                  (const double*)net_ptrs[3], (const double*)net_ptrs[4], (const double*)net_ptrs[5],
+                  (const double*)net_ptrs[6]};
+    net = &nf64;
+  }
+  LdArgs la{};
+  la.rec = (const PropRec*)rec;
+  la.prop_occ = prop_occ;
+  la.occ = occ;
+  la.nacc = n_acc;
+  la.z0 = z0;
+  la.w0t = prec == 0 ? (const void*)nf32.w0t : (const void*)nf64.w0t;
+  la.sign = sign;
+  la.logabs = logabs;
+  for (int s = 0; s < n_sweeps; ++s) {
+    for (int e = 0; e < n_edges; ++e) {
+      if (prec == 0)
+        k_prep_sweep<float><<<gw, 256, 0, st>>>(B, n_sites, occ, edges, e, s, n_edges, hopping_rate, seed,
+                                                sweep_offset + (uint64_t)s, r_move, r_bit, r_acc, (const float*)z0,
+                                                nf32.w0t, prop_occ, (PropRec*)rec, H1);
+      else
+        k_prep_sweep<double><<<gw, 256, 0, st>>>(B, n_sites, occ, edges, e, s, n_edges, hopping_rate, seed,
+                                                 sweep_offset + (uint64_t)s, r_move, r_bit, r_acc,
+                                                 (const double*)z0, nf64.w0t, prop_occ, (PropRec*)rec, H1);
+      int rc = launch_eval_rows(prec, B, n_sites, nf, prop_occ, net, bf_scale, Work{H1, H2, A}, d_err, st,
+                                LD_ACCEPT, la);
+      if (rc) return rc;
+    }
+  }
+  VMC_CUDA_CHECK_LAUNCH();
+  return VMC_OK;
+}
+
+// Local energy.  pairs/offs come from vmc_nnbf_conn_pairs; chunk rows at a time
+// are evaluated with the workspace (H1, H2, A sized for `chunk` rows).
+int vmc_nnbf_conn_count(const uint64_t* occ, int64_t B, int n_sites, const int32_t* edges, int n_edges, int32_t* cnt,
+                        void* stream) {
+  if (B < 0 || n_sites < 1 || n_sites > 64 || n_edges < 0 || (B > 0 && (!occ || !cnt || !edges))) return VMC_ERR_ARGS;
+  if (B == 0) return VMC_OK;
+  k_count_hops<<<(unsigned)((B + 255) / 256), 256, 0, (cudaStream_t)stream>>>(B, n_sites, occ, edges, n_edges, cnt);
+  VMC_CUDA_CHECK_LAUNCH();
+  return VMC_OK;
+}
+
+int vmc_nnbf_conn_pairs(const uint64_t* occ, int64_t B, int n_sites, const int32_t* edges, int n_edges,
+                        const int32_t* offs, int32_t* pairs, void* stream) {
+  if (B < 0 || n_sites < 1 || n_sites > 64 || n_edges < 0 || (B > 0 && (!occ || !offs || !pairs || !edges)))
+    return VMC_ERR_ARGS;
+  if (B == 0) return VMC_OK;
+  k_fill_pairs<<<(unsigned)((B + 255) / 256), 256, 0, (cudaStream_t)stream>>>(B, n_sites, occ, edges, n_edges, offs,
+                                                                            pairs);
+  VMC_CUDA_CHECK_LAUNCH();
+  return VMC_OK;
+}
+
+int vmc_nnbf_local_energy(int prec, const void* const* net_ptrs, int n_sites, int nf, int hidden, double bf_scale,
+                          const uint64_t* occ, int64_t B, const int32_t* edges, double t, double U, const void* z0,
+                          const double* sign, const double* logabs, const int32_t* pairs, const int32_t* offs,
+                          int64_t P, int64_t chunk, uint64_t* row_occ, double* coeff, double* term, void* H1, void* H2,
+                          void* A, double* eloc, int* d_err, void* stream) {
+  int st0 = check_shape(prec, n_sites, nf, hidden);
+  if (st0) return st0;
+  if (B < 0 || P < 0 || chunk <= 0) return VMC_ERR_ARGS;
+  if (B == 0) return VMC_OK;
+  if (!net_ptrs || !occ || !z0 || !sign || !logabs || !offs || !eloc || !d_err || !row_occ || !coeff || !term ||
+      !H1 || !H2 || !A || (P > 0 && (!pairs || !edges)))
+    return VMC_ERR_ARGS;
+  set_attrs();
+  cudaStream_t st = (cudaStream_t)stream;
+  NetF32 nf32; NetF64 nf64;
+  const void* net;
+  if (prec == 0) {
+    nf32 = NetF32{(const float*)net_ptrs[0], (const float*)net_ptrs[1], (const __nv_bfloat16*)net_ptrs[2],
+                  (const float*)net_ptrs[3], (const __nv_bfloat16*)net_ptrs[4], (const float*)net_ptrs[5],
+                  (const float*)net_ptrs[6]};
+    net = &nf32;
+  } else {
+    nf64 = NetF64{(const double*)net_ptrs[0], (const double*)net_ptrs[1], (const double*)net_ptrs[2],
+                  (const double*)net_ptrs[3], (const double*)net_ptrs[4], (const double*)net_ptrs[5],
+                  (const double*)net_ptrs[6]};
+    net = &nf64;
+  }
+  for (int64_t p0 = 0; p0 < P; p0 += chunk) {
+    const int64_t R = (P - p0) < chunk ? (P - p0) : chunk;
+    const unsigned gw = (unsigned)((R * 32 + 255) / 256);
+    if (prec == 0)
+      k_prep_conn<float><<<gw, 256, 0, st>>>(R, n_sites, pairs + 2 * p0, occ, edges, t, (const float*)z0, nf32.w0t,
+                                             row_occ, coeff, H1);
+    else
+      k_prep_conn<double><<<gw, 256, 0, st>>>(R, n_sites, pairs + 2 * p0, occ, edges, t, (const double*)z0, nf64.w0t,
+                                              row_occ, coeff, H1);
+    LdArgs la{};
+    la.pairs = pairs + 2 * p0;
+    la.coeff = coeff;
+    la.term = term + p0;
+    la.sign = const_cast<double*>(sign);
+    la.logabs = const_cast<double*>(logabs);
+    int rc = launch_eval_rows(prec, R, n_sites, nf, row_occ, net, bf_scale, Work{H1, H2, A}, d_err, st, LD_ELOC, la);
+    if (rc) return rc;
+  }
+  k_eloc_reduce<<<(unsigned)((B + 255) / 256), 256, 0, st>>>(B, occ, offs, term, U, eloc);
+  VMC_CUDA_CHECK_LAUNCH();
+  return VMC_OK;
+}
+
+}  // extern "C"

@@ -9,6 +9,8 @@ keeps one persistent walker state (packed occupations plus the per-walker
 amplitude data the kernels update in place) bound to the configuration tensor
 it last saw; sampler, local energy and gradients share it.
 """
+import ctypes
+
 import torch
 import torch.nn as nn
 
@@ -207,3 +209,171 @@ class SlaterDeterminant_GB300(WavefunctionModel_GB300):
         _lib.call("vmc_slater_logpsi_grad", _lib.ptr(st.extra["G"]), _lib.ptr(st.extra["slot"]), st.B,
                   self.n_orbitals, self.n_fermions, _lib.ptr(out), out.stride(0), _lib.stream_of(st.device))
         return out
+
+
+_PREC = {"mixed": 0, "fp64": 1}
+
+
+class NNBF_GB300(WavefunctionModel_GB300):
+    """Neural-network backflow psi(x) = det((M_base + bf_scale * MLP(n))[occ])
+    (vmc_torch/GPU/models/NNBF.py:36-162) with GELU hidden layers of width 256.
+
+    Parameters (FP64 masters, reference order): M_base (2N, N_f), w_0 (H, 2N),
+    b_0 (H), w_1 (H, H), b_1 (H), out_w (2N*N_f, H), out_b (2N*N_f).
+
+    precision="mixed": BF16 tensor-core MLP with FP32 accumulation, FP32
+    determinant, log|det| combined in FP64 (the production path).
+    precision="fp64": every stage in FP64 (parity mode, 1e-10 against the oracle).
+
+    init="fan_in": M_base ~ N(0, 0.1^2), weights ~ N(0, 1/fan_in), biases 0;
+    init="reference": the reference's defaults (M_base ~ N(0,1), kaiming-uniform
+    hidden weights, zero output layer).
+    """
+
+    def __init__(self, n_sites, n_fermions, hidden_dim=256, n_layers=2, activation="gelu", bf_scale=0.01,
+                 dtype=torch.float64, precision="mixed", init="fan_in", generator=None):
+        if hidden_dim != 256 or n_layers != 2 or activation != "gelu":
+            raise ValueError("the GB300 NNBF kernels implement 2 GELU hidden layers of width 256")
+        if precision not in _PREC:
+            raise ValueError("precision must be 'mixed' or 'fp64'")
+        n_orb = 2 * n_sites
+        g = generator
+        if init == "fan_in":
+            ps = [torch.randn(n_orb, n_fermions, generator=g, dtype=torch.float64) * 0.1]
+            fan = n_orb
+            for _ in range(n_layers):
+                ps.append(torch.randn(hidden_dim, fan, generator=g, dtype=torch.float64) / fan ** 0.5)
+                ps.append(torch.zeros(hidden_dim, dtype=torch.float64))
+                fan = hidden_dim
+            ps.append(torch.randn(n_orb * n_fermions, fan, generator=g, dtype=torch.float64) / fan ** 0.5)
+            ps.append(torch.zeros(n_orb * n_fermions, dtype=torch.float64))
+        elif init == "reference":
+            ps = [torch.randn(n_orb, n_fermions, generator=g, dtype=torch.float64)]
+            fan = n_orb
+            for _ in range(n_layers):
+                w = torch.empty(hidden_dim, fan, dtype=torch.float64)
+                torch.nn.init.kaiming_uniform_(w, a=0, mode="fan_in", nonlinearity="tanh", generator=g)
+                ps += [w, torch.zeros(hidden_dim, dtype=torch.float64)]
+                fan = hidden_dim
+            ps += [torch.zeros(n_orb * n_fermions, fan, dtype=torch.float64),
+                   torch.zeros(n_orb * n_fermions, dtype=torch.float64)]
+        else:
+            raise ValueError("init must be 'fan_in' or 'reference'")
+        super().__init__(ps, n_sites)
+        self.n_fermions = n_fermions
+        self.n_orbitals = n_orb
+        self.hidden_dim = hidden_dim
+        self.n_layers = n_layers
+        self.bf_scale = float(bf_scale)
+        self.precision = precision
+        self._net_cache = None
+        self.refresh_each_sweep = True
+
+    # ---- device copies of the parameters in kernel layout ----
+    def net(self, device):
+        key = (self.param_key(), str(device), self.precision)
+        if self._net_cache is not None and self._net_cache[0] == key:
+            return self._net_cache[1]
+        p = [q.detach() for q in self.params]
+        if any(q.device != device for q in p):
+            raise ValueError("model parameters must live on the walkers' device (call model.to(device))")
+        M_base, w0, b0, w1, b1, out_w, out_b = p
+        if self.precision == "mixed":
+            f32, bf = torch.float32, torch.bfloat16
+            ts = [w0.t().contiguous().to(f32), b0.to(f32).contiguous(), w1.to(bf).contiguous(),
+                  b1.to(f32).contiguous(), out_w.to(bf).contiguous(), out_b.to(f32).contiguous(),
+                  M_base.to(f32).contiguous()]
+        else:
+            ts = [w0.t().contiguous(), b0.contiguous(), w1.contiguous(), b1.contiguous(), out_w.contiguous(),
+                  out_b.contiguous(), M_base.contiguous()]
+        arr = (ctypes.c_void_p * 7)(*[t.data_ptr() for t in ts])
+        self._net_cache = (key, (ts, arr))
+        return ts, arr
+
+    @property
+    def _prec(self):
+        return _PREC[self.precision]
+
+    def _hdtype(self):
+        return torch.bfloat16 if self.precision == "mixed" else torch.float64
+
+    def _rdtype(self):
+        return torch.float32 if self.precision == "mixed" else torch.float64
+
+    def _new_state(self, B, device):
+        st = WalkerState(B, self.n_sites, device)
+        nf, H = self.n_fermions, self.hidden_dim
+        x = st.extra
+        x["z0"] = torch.empty((B, H), dtype=self._rdtype(), device=device)
+        x["prop_occ"] = torch.zeros((B, 2), dtype=torch.int64, device=device)
+        x["rec"] = torch.zeros((B, 4), dtype=torch.int32, device=device)
+        x["H1"] = torch.empty((B, H), dtype=self._hdtype(), device=device)
+        x["H2"] = torch.empty((B, H), dtype=self._hdtype(), device=device)
+        x["A"] = torch.empty((B, nf, nf), dtype=self._rdtype(), device=device)
+        x["err"] = torch.zeros(1, dtype=torch.int32, device=device)
+        return st
+
+    def _check_err(self, st):
+        if int(st.extra["err"].item()) != 0:
+            v = int(st.extra["err"].item())
+            st.extra["err"].zero_()
+            raise RuntimeError("NNBF kernel reported status %d (a bounded device wait gave up)" % v)
+
+    def _refresh(self, st, threshold):
+        ts, arr = self.net(st.device)
+        x = st.extra
+        _lib.call("vmc_nnbf_eval", self._prec, arr, self.n_sites, self.n_fermions, self.hidden_dim, self.bf_scale,
+                  _lib.ptr(st.occ), st.B, _lib.ptr(x["z0"]), _lib.ptr(x["H1"]), _lib.ptr(x["H2"]), _lib.ptr(x["A"]),
+                  _lib.ptr(st.sign), _lib.ptr(st.logabs), _lib.ptr(x["err"]), _lib.stream_of(st.device))
+        st.n_acc.zero_()
+
+    def sweep(self, st, graph, n_sweeps, seed, sweep_offset, hopping_rate=0.25, replay=None):
+        from .hamiltonian import device_sweep_edges
+        ts, arr = self.net(st.device)
+        edges = device_sweep_edges(graph, st.device)
+        rm = rb = ra = None
+        if replay is not None:
+            rm, rb, ra = replay
+            E = edges.shape[0]
+            for a in (rm, rb, ra):
+                if tuple(a.shape) != (n_sweeps, E, st.B) or not a.is_cuda or not a.is_contiguous():
+                    raise ValueError("replay buffers must be contiguous CUDA tensors of shape (n_sweeps, E, B)")
+        if self.refresh_each_sweep:
+            self._refresh(st, 0)  # recompute z0 = W0 n + b0 and psi from scratch (resets FP32 drift)
+        x = st.extra
+        _lib.call("vmc_nnbf_sweep", self._prec, arr, self.n_sites, self.n_fermions, self.hidden_dim, self.bf_scale,
+                  _lib.ptr(st.occ), st.B, _lib.ptr(edges), edges.shape[0], int(n_sweeps), float(hopping_rate),
+                  int(seed) & ((1 << 64) - 1), int(sweep_offset), _lib.ptr(rm), _lib.ptr(rb), _lib.ptr(ra),
+                  _lib.ptr(x["z0"]), _lib.ptr(st.sign), _lib.ptr(st.logabs), _lib.ptr(st.n_acc),
+                  _lib.ptr(x["prop_occ"]), _lib.ptr(x["rec"]), _lib.ptr(x["H1"]), _lib.ptr(x["H2"]),
+                  _lib.ptr(x["A"]), _lib.ptr(x["err"]), _lib.stream_of(st.device))
+
+    def conn_pairs(self, st, H):
+        edges = H.edges_on(st.device)
+        cnt = torch.empty(st.B, dtype=torch.int32, device=st.device)
+        _lib.call("vmc_nnbf_conn_count", _lib.ptr(st.occ), st.B, self.n_sites, _lib.ptr(edges), edges.shape[0],
+                  _lib.ptr(cnt), _lib.stream_of(st.device))
+        offs = torch.zeros(st.B + 1, dtype=torch.int32, device=st.device)
+        offs[1:] = torch.cumsum(cnt, 0)
+        P = int(offs[-1].item())
+        pairs = torch.empty((max(P, 1), 2), dtype=torch.int32, device=st.device)
+        _lib.call("vmc_nnbf_conn_pairs", _lib.ptr(st.occ), st.B, self.n_sites, _lib.ptr(edges), edges.shape[0],
+                  _lib.ptr(offs), _lib.ptr(pairs), _lib.stream_of(st.device))
+        return pairs, offs, P
+
+    def local_energy(self, st, H):
+        ts, arr = self.net(st.device)
+        edges = H.edges_on(st.device)
+        pairs, offs, P = self.conn_pairs(st, H)
+        x = st.extra
+        chunk = st.B
+        row_occ = torch.empty((chunk, 2), dtype=torch.int64, device=st.device)
+        coeff = torch.empty(chunk, dtype=torch.float64, device=st.device)
+        term = torch.empty(max(P, 1), dtype=torch.float64, device=st.device)
+        eloc = torch.empty(st.B, dtype=torch.float64, device=st.device)
+        _lib.call("vmc_nnbf_local_energy", self._prec, arr, self.n_sites, self.n_fermions, self.hidden_dim,
+                  self.bf_scale, _lib.ptr(st.occ), st.B, _lib.ptr(edges), float(H.t), float(H.U), _lib.ptr(x["z0"]),
+                  _lib.ptr(st.sign), _lib.ptr(st.logabs), _lib.ptr(pairs), _lib.ptr(offs), P, chunk,
+                  _lib.ptr(row_occ), _lib.ptr(coeff), _lib.ptr(term), _lib.ptr(x["H1"]), _lib.ptr(x["H2"]),
+                  _lib.ptr(x["A"]), _lib.ptr(eloc), _lib.ptr(x["err"]), _lib.stream_of(st.device))
+        return eloc
