@@ -1,0 +1,323 @@
+"""Benchmark of the VMC inner loop on one GB300.
+
+Workload (the headline configuration): 8x8 OBC spinful Fermi-Hubbard, t=1,
+U=8, 32 up + 32 down electrons; neural-backflow Slater determinant (128-dim
+occupation -> 2 x 256 GELU -> 128 x 64 orbital correction, N(0, 1/fan_in)
+init, bf_scale 0.01) with the MLP in BF16 / FP32 accumulation and the
+determinant in FP32; 16384 walkers resident on the GPU.
+
+A step is one Metropolis sweep of every walker over all 112 nearest-neighbour
+edges (exchange-or-hop proposals, 25 % hops), i.e. 16384 * 112 walker-steps.
+``value`` is walker-steps/s with the walkers resident in HBM; ``e2e`` is the
+same metric through the public sampler API with the configurations copied
+from pinned host memory before each step and the configurations plus
+log-amplitudes copied back after it.  L2 is flushed (256 MB write) between
+timed steps.
+
+--impl reference times the reference algorithm on the host CPU: the CPU port
+of the reference's batched sampler (oracle/sampler.py with the FP64 NNBF
+amplitude of oracle/models.py), on a bounded sample of walkers per step.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "walker-steps/s and ESS/s, learned vs plain proposal, at |ΔE/site|<1e-3"
+UNIT = "walker-steps/s"
+LX, LY, NUP, NDN = 8, 8, 32, 32
+B = 16384
+HID = 256
+BF_SCALE = 0.01
+
+
+def workload_config(extra=None):
+    cfg = {"workload": "8x8 OBC Fermi-Hubbard t=1 U=8 (32+32), NNBF 2x256 GELU backflow, 16384 walkers, "
+                       "one exchange-or-hop Metropolis sweep (112 edges) per step",
+           "lattice": "8x8", "n_up": NUP, "n_dn": NDN, "walkers": B, "hidden": "2x256", "edges_per_sweep": 112,
+           "mlp_dtype": "bf16 (fp32 accumulate)", "det_dtype": "fp32", "init": "N(0,1/fan_in), M_base N(0,0.1^2)",
+           "l2": "flushed (256 MB write) between timed steps", "parallelism": "replicas (1 GPU per process)"}
+    if extra:
+        cfg.update(extra)
+    return cfg
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[4:8]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return {"hbm_gbs": d.get("hbm_gbs"), "bf16_tflops": d.get("bf16_tflops"),
+                "bf16_tflops_sustained": d.get("bf16_tflops_sustained"), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0, "source": "fallback"}
+
+
+# ---------------------------------------------------------------------------
+def cpu_port_rate(n_walkers=48, n_sweeps=1, seed=0):
+    """The oracle (CPU port of the reference sampler + FP64 NNBF) on a bounded
+    sample: returns (walker-steps/s, seconds, sample description)."""
+    from oracle import lattice, models, sampler
+    ps = models.nnbf_init(LX * LY, NUP + NDN, HID, 2, seed=seed)
+    edges = lattice.sweep_edges(LX, LY)
+    X = lattice.random_initial_configs(n_walkers, LX * LY, NUP, NDN, seed=seed + 1)
+    rng = np.random.default_rng(seed + 2)
+    S, E = n_sweeps, len(edges)
+    um = rng.random((S, E, n_walkers), dtype=np.float32)
+    hb = rng.integers(0, 2, (S, E, n_walkers)).astype(np.uint8)
+    ua = rng.random((S, E, n_walkers), dtype=np.float32)
+    t0 = time.perf_counter()
+    sampler.sweep(X, edges, lambda y: models.nnbf_logamp(ps, y, BF_SCALE), um, hb, ua)
+    dt = time.perf_counter() - t0
+    steps = n_walkers * E * S
+    return steps / dt, dt, "%d walkers x %d sweep(s) x %d edges of the same 8x8 NNBF workload (FP64 numpy)" % (
+        n_walkers, S, E)
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    cores = os.cpu_count()
+    for _ in range(args.warmup):
+        cpu_port_rate(n_walkers=16, n_sweeps=1)
+    rates, tot = [], 0.0
+    for k in range(args.steps):
+        r, dt, sample = cpu_port_rate(n_walkers=48, n_sweeps=1, seed=k)
+        rates.append(r)
+        tot += dt
+    value = float(np.mean(rates))
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": workload_config({"sample": sample}), "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+def run_gb300(args):
+    import torch
+    import vmc_torch_gb300 as vg
+    from vmc_torch_gb300 import build as vbuild
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    if not os.path.exists(vbuild.LIB):
+        vbuild.build()
+
+    gen = torch.Generator().manual_seed(1234 + rank)
+    model = vg.NNBF_GB300(LX * LY, NUP + NDN, hidden_dim=HID, n_layers=2, bf_scale=BF_SCALE, precision="mixed",
+                          generator=gen).to(dev)
+    H = vg.spinful_Fermi_Hubbard_square_lattice_torch(LX, LY, 1.0, 8.0, NUP + NDN, n_fermions_per_spin=(NUP, NDN))
+    H.precompute_hops_gpu(dev)
+    graph = H.graph
+    E = len(graph.sweep_edges())
+    fxs = vg.init_walkers(B, LX * LY, NUP, NDN, seed=7 + 1000 * rank, device=dev)
+    smp = vg.MetropolisExchangeSpinfulSamplerGB300(seed=11 + rank)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    # burn-in + warm-up (untimed)
+    smp.burn_in(fxs, model, graph, 2, use_log_amp=True)
+    for _ in range(args.warmup):
+        smp.step(fxs, model, graph, use_log_amp=True)
+    torch.cuda.synchronize()
+
+    # ---- device-resident timed region ----
+    instr = {}
+    st = model.bind_state(fxs)
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clk = ClockSampler(local)
+    clk.start()
+    time.sleep(0.3)
+    total_ms = 0.0
+    stream = torch.cuda.current_stream(dev)
+    for k in range(args.steps):
+        flush.fill_(float(k))
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        smp.step(fxs, model, graph, use_log_amp=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        total_ms += e0.elapsed_time(e1)
+    torch.cuda.synchronize()
+    clocks = clk.stop()
+    # same steps again with CUDA events around every kernel launch (per-kernel
+    # device time on the launching stream) for the roofline / kernel shares
+    for k in range(args.steps):
+        flush.fill_(float(k))
+        torch.cuda.synchronize()
+        smp.step(fxs, model, graph, use_log_amp=True, instrument=instr)
+    torch.cuda.synchronize()
+    t_max = torch.tensor([total_ms], device=dev)
+    if dist is not None:
+        dist.all_reduce(t_max, op=dist.ReduceOp.MAX)
+        dist.barrier()
+    total_ms = float(t_max.item())
+    wsteps = args.steps * B * E
+    value = wsteps * world / (total_ms / 1e3)
+    n_eval = int(instr["n_eval"].item())
+    stage_ms = list(instr["stage_ms"])
+    stage_n = list(instr["stage_launches"])
+    eloc_check = None
+
+    # ---- roofline of the dominant kernel (device time share inside the timed region) ----
+    names = ["prep (proposal + first layer)", "hidden layer GEMM (tcgen05)", "backflow GEMM (tcgen05, persistent)",
+             "LU log-det + accept (FP32 CUDA cores)"]
+    pk = peaks()
+    nf = NUP + NDN
+    # algorithmic work per launch
+    lu_flops = n_eval * (2.0 / 3.0) * nf ** 3
+    bf_flops = args.steps * E * B * 2.0 * HID * (2 * LX * LY * nf)
+    l1_flops = args.steps * E * B * 2.0 * HID * HID
+    per_kernel = []
+    for i, (nm, ms, n) in enumerate(zip(names, stage_ms, stage_n)):
+        per_kernel.append({"kernel": nm, "launches": n, "ms_total": ms, "share": ms / max(sum(stage_ms), 1e-9)})
+    dom = int(np.argmax(stage_ms))
+    kern_flops = [0.0, l1_flops, bf_flops, lu_flops]
+    achieved = kern_flops[dom] / (stage_ms[dom] / 1e3) / 1e12
+    roofline = {"bound": "tensor", "achieved": achieved, "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
+                "frac": achieved / pk["bf16_tflops"], "traffic": None,
+                "kernel": names[dom], "peak_source": pk["source"] + " (bf16 burst, MEASURED_PEAKS.json)",
+                "algorithmic": "LU: (2/3) nf^3 FLOP per evaluated proposal (nf=64); GEMMs: 2*M*N*K",
+                "per_kernel": per_kernel,
+                "backflow_gemm_tflops": bf_flops / (stage_ms[2] / 1e3) / 1e12 if stage_ms[2] else None,
+                "hidden_gemm_tflops": l1_flops / (stage_ms[1] / 1e3) / 1e12 if stage_ms[1] else None}
+
+    # ---- end-to-end through the public API with host buffers ----
+    host_fx = torch.empty((B, LX * LY), dtype=torch.int64).pin_memory()
+    host_fx.copy_(fxs.cpu())
+    host_la = torch.empty(B, dtype=torch.float64).pin_memory()
+    host_sg = torch.empty(B, dtype=torch.float64).pin_memory()
+    dev_fx = torch.empty_like(fxs)
+    torch.cuda.synchronize()
+    e2e_ms = 0.0
+    for k in range(args.steps):
+        flush.fill_(float(k))
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        dev_fx.copy_(host_fx, non_blocking=True)
+        _, (sg, la) = smp.step(dev_fx, model, graph, use_log_amp=True)
+        host_fx.copy_(dev_fx, non_blocking=True)
+        host_sg.copy_(sg, non_blocking=True)
+        host_la.copy_(la, non_blocking=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        e2e_ms += e0.elapsed_time(e1)
+    e2e_value = args.steps * B * E * world / (e2e_ms / 1e3)
+    h2d = B * LX * LY * 8
+    d2h = B * LX * LY * 8 + 2 * B * 8
+    n_chunks = -(-B // 4096)
+    # per step: the instrumented sweep launches + the per-call refresh (prep, hidden GEMM,
+    # n_chunks x (backflow GEMM + LU)) + the unpack of the configurations
+    gpu_launches = sum(stage_n) + args.steps * (2 + 2 * n_chunks + 1)
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        r, dt, sample = cpu_port_rate(n_walkers=48, n_sweeps=1)
+        cpu = {"value": r, "unit": UNIT, "cores": os.cpu_count(), "kind": "port", "sample": sample,
+               "seconds": dt}
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "bf16 MLP / fp32 det",
+                "data": "synthetic (seeded walkers and random-init weights)",
+                "config": workload_config({"accepted_per_walker_per_step":
+                                           float(st.n_acc.float().mean().item()) if st is not None else None,
+                                           "evaluated_proposals_per_step": n_eval / args.steps}),
+                "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+                "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": gpu_launches}
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gb300(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -21,6 +21,7 @@
 // An FP64 twin of every stage (CUDA cores) gives the 1e-10 parity mode.
 #include <cuda_bf16.h>
 #include <utility>
+#include <vector>
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include "common.cuh"
@@ -732,6 +733,7 @@ struct LdArgs {
   // accept / eval
   double* sign;
   double* logabs;
+  unsigned long long* n_eval;  // accept mode: number of proposals evaluated (nullable)
   // eloc
   const int32_t* pairs;
   const double* coeff;
@@ -747,6 +749,7 @@ __global__ void k_logdet(int64_t R, int64_t row0, int nf, const T* __restrict__ 
   const int64_t row = row0 + local;
   if (MODE == LD_ACCEPT) {
     if (!la.rec[row].flag) return;
+    if (la.n_eval && lane == 0) atomicAdd(la.n_eval, 1ull);
   }
   Det d;
   if constexpr (sizeof(T) == 4) {
@@ -880,6 +883,45 @@ struct Work {
   void* H1; void* H2; void* A;
 };
 
+// Optional per-stage device timing (CUDA events on the launching stream),
+// used by the benchmark to time the kernels inside its timed region.
+struct StageTimer {
+  cudaStream_t st = nullptr;
+  float* acc = nullptr;  // host: [prep, layer1, backflow, logdet] milliseconds
+  int* cnt = nullptr;    // host: launches per stage
+  std::vector<cudaEvent_t> ev;
+  std::vector<int> stage;
+  size_t used = 0;
+  void begin() {}
+  void mark(int stg, bool start) {
+    if (!acc) return;
+    if (used == ev.size()) {
+      cudaEvent_t e;
+      cudaEventCreate(&e);
+      ev.push_back(e);
+      stage.push_back(0);
+    }
+    stage[used] = start ? stg : -1;
+    cudaEventRecord(ev[used], st);
+    ++used;
+  }
+  void finish() {
+    if (!acc) return;
+    cudaStreamSynchronize(st);
+    for (size_t i = 0; i + 1 < used; i += 2) {
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, ev[i], ev[i + 1]) == cudaSuccess) {
+        acc[stage[i]] += ms;
+        cnt[stage[i]] += 1;
+      }
+    }
+    used = 0;
+  }
+};
+StageTimer g_timer;
+#define STAGE_BEGIN(s) g_timer.mark((s), true)
+#define STAGE_END(s) g_timer.mark((s), false)
+
 // Rows per backflow+LU chunk: 4096 x 64 x 64 FP32 orbital matrices = 64 MB,
 // small enough to stay resident in L2 between the GEMM epilogue and the LU.
 constexpr int64_t kChunkRows = 4096;
@@ -910,7 +952,9 @@ int launch_eval_rows(int prec, int64_t R, int N, int nf, const uint64_t* row_occ
     e1.bias = n.b1;
     e1.out = (__nv_bfloat16*)wk.H2;
     dim3 g1((unsigned)((R + TM - 1) / TM), 1);
+    STAGE_BEGIN(1);
     k_gemm_tc<EPI_GELU_BF16><<<g1, 128, GEMM_SMEM, st>>>(tH1, tW1, (int)R, e1, err);
+    STAGE_END(1);
     const int n_groups = (n_orb * nf) / TN;
     const int64_t CH = R < kChunkRows ? R : kChunkRows;
     const int wpb = 4;
@@ -925,7 +969,10 @@ int launch_eval_rows(int prec, int64_t R, int N, int nf, const uint64_t* row_occ
       pa.n_tiles = (int)((Rc + TM - 1) / TM);
       pa.n_items = n_groups * pa.n_tiles;
       const int grid = pa.n_items < num_sms() ? pa.n_items : num_sms();
+      STAGE_BEGIN(2);
       k_backflow_persistent<<<grid, PB_THREADS, PB_SMEM, st>>>(tH2c, tOW, pa, err);
+      STAGE_END(2);
+      STAGE_BEGIN(3);
       const unsigned gl = (unsigned)((Rc + wpb - 1) / wpb);
       if (nf == 64) {
         if (ldmode == LD_ACCEPT) k_logdet<float, 64, LD_ACCEPT><<<gl, 32 * wpb, lsmem, st>>>(Rc, c0, nf, (const float*)wk.A, la);
@@ -936,6 +983,7 @@ int launch_eval_rows(int prec, int64_t R, int N, int nf, const uint64_t* row_occ
         else if (ldmode == LD_EVAL) k_logdet<float, 32, LD_EVAL><<<gl, 32 * wpb, lsmem, st>>>(Rc, c0, nf, (const float*)wk.A, la);
         else k_logdet<float, 32, LD_ELOC><<<gl, 32 * wpb, lsmem, st>>>(Rc, c0, nf, (const float*)wk.A, la);
       }
+      STAGE_END(3);
     }
   } else {
     const NetF64& n = *(const NetF64*)net;
@@ -1017,7 +1065,8 @@ int vmc_nnbf_sweep(int prec, const void* const* net_ptrs, int n_sites, int nf, i
                    uint64_t* occ, int64_t B, const int32_t* edges, int n_edges, int n_sweeps, float hopping_rate,
                    uint64_t seed, uint64_t sweep_offset, const float* r_move, const uint8_t* r_bit, const float* r_acc,
                    void* z0, double* sign, double* logabs, int32_t* n_acc, uint64_t* prop_occ, void* rec, void* H1,
-                   void* H2, void* A, int* d_err, void* stream) {
+                   void* H2, void* A, int* d_err, unsigned long long* d_n_eval, float* stage_ms, int* stage_launches,
+                   void* stream) {
   int st0 = check_shape(prec, n_sites, nf, hidden);
   if (st0) return st0;
   if (B < 0 || n_edges < 0 || n_sweeps < 0) return VMC_ERR_ARGS;
@@ -1051,8 +1100,14 @@ int vmc_nnbf_sweep(int prec, const void* const* net_ptrs, int n_sites, int nf, i
   la.w0t = prec == 0 ? (const void*)nf32.w0t : (const void*)nf64.w0t;
   la.sign = sign;
   la.logabs = logabs;
+  la.n_eval = d_n_eval;
+  g_timer.st = st;
+  g_timer.acc = stage_ms;
+  g_timer.cnt = stage_launches;
+  g_timer.used = 0;
   for (int s = 0; s < n_sweeps; ++s) {
     for (int e = 0; e < n_edges; ++e) {
+      STAGE_BEGIN(0);
       if (prec == 0)
         k_prep_sweep<float><<<gw, 256, 0, st>>>(B, n_sites, occ, edges, e, s, n_edges, hopping_rate, seed,
                                                 sweep_offset + (uint64_t)s, r_move, r_bit, r_acc, (const float*)z0,
@@ -1061,11 +1116,14 @@ int vmc_nnbf_sweep(int prec, const void* const* net_ptrs, int n_sites, int nf, i
         k_prep_sweep<double><<<gw, 256, 0, st>>>(B, n_sites, occ, edges, e, s, n_edges, hopping_rate, seed,
                                                  sweep_offset + (uint64_t)s, r_move, r_bit, r_acc,
                                                  (const double*)z0, nf64.w0t, prop_occ, (PropRec*)rec, H1);
+      STAGE_END(0);
       int rc = launch_eval_rows(prec, B, n_sites, nf, prop_occ, net, bf_scale, Work{H1, H2, A}, d_err, st,
                                 LD_ACCEPT, la);
-      if (rc) return rc;
+      if (rc) { g_timer.acc = nullptr; return rc; }
     }
   }
+  g_timer.finish();
+  g_timer.acc = nullptr;
   VMC_CUDA_CHECK_LAUNCH();
   return VMC_OK;
 }

@@ -327,7 +327,9 @@ class NNBF_GB300(WavefunctionModel_GB300):
                   _lib.ptr(st.sign), _lib.ptr(st.logabs), _lib.ptr(x["err"]), _lib.stream_of(st.device))
         st.n_acc.zero_()
 
-    def sweep(self, st, graph, n_sweeps, seed, sweep_offset, hopping_rate=0.25, replay=None):
+    def sweep(self, st, graph, n_sweeps, seed, sweep_offset, hopping_rate=0.25, replay=None, instrument=None):
+        """instrument: optional dict; receives 'n_eval' (device counter) and
+        accumulates 'stage_ms'/'stage_launches' (host arrays of 4) per stage."""
         from .hamiltonian import device_sweep_edges
         ts, arr = self.net(st.device)
         edges = device_sweep_edges(graph, st.device)
@@ -346,7 +348,18 @@ class NNBF_GB300(WavefunctionModel_GB300):
                   int(seed) & ((1 << 64) - 1), int(sweep_offset), _lib.ptr(rm), _lib.ptr(rb), _lib.ptr(ra),
                   _lib.ptr(x["z0"]), _lib.ptr(st.sign), _lib.ptr(st.logabs), _lib.ptr(st.n_acc),
                   _lib.ptr(x["prop_occ"]), _lib.ptr(x["rec"]), _lib.ptr(x["H1"]), _lib.ptr(x["H2"]),
-                  _lib.ptr(x["A"]), _lib.ptr(x["err"]), _lib.stream_of(st.device))
+                  _lib.ptr(x["A"]), _lib.ptr(x["err"]), *self._instr_args(instrument, st.device),
+                  _lib.stream_of(st.device))
+
+    @staticmethod
+    def _instr_args(instrument, device):
+        if instrument is None:
+            return (None, None, None)
+        if "n_eval" not in instrument:
+            instrument["n_eval"] = torch.zeros(1, dtype=torch.int64, device=device)
+            instrument["stage_ms"] = (ctypes.c_float * 4)()
+            instrument["stage_launches"] = (ctypes.c_int * 4)()
+        return (_lib.ptr(instrument["n_eval"]), instrument["stage_ms"], instrument["stage_launches"])
 
     def conn_pairs(self, st, H):
         edges = H.edges_on(st.device)

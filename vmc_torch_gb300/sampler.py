@@ -45,9 +45,13 @@ class MetropolisExchangeSpinfulSamplerGB300(SamplerGB300):
         self.sweeps_per_step = sweeps_per_step
         self.sweep_counter = 0
 
-    def _run(self, fxs, model, graph, n_sweeps, use_log_amp, replay):
+    def _run(self, fxs, model, graph, n_sweeps, use_log_amp, replay, instrument=None):
         st = model.bind_state(fxs)
-        model.sweep(st, graph, n_sweeps, self.seed, self.sweep_counter, self.hopping_rate, replay)
+        if instrument is None:
+            model.sweep(st, graph, n_sweeps, self.seed, self.sweep_counter, self.hopping_rate, replay)
+        else:
+            model.sweep(st, graph, n_sweeps, self.seed, self.sweep_counter, self.hopping_rate, replay,
+                        instrument=instrument)
         self.sweep_counter += n_sweeps
         model.store_configs(st, fxs)
         if use_log_amp:
@@ -55,8 +59,9 @@ class MetropolisExchangeSpinfulSamplerGB300(SamplerGB300):
         return fxs, st.sign * torch.exp(st.logabs)
 
     @torch.inference_mode()
-    def step(self, fxs, model, graph, compile=False, verbose=False, use_log_amp=False, replay=None, **kwargs):
-        return self._run(fxs, model, graph, self.sweeps_per_step, use_log_amp, replay)
+    def step(self, fxs, model, graph, compile=False, verbose=False, use_log_amp=False, replay=None, instrument=None,
+             **kwargs):
+        return self._run(fxs, model, graph, self.sweeps_per_step, use_log_amp, replay, instrument)
 
     @torch.inference_mode()
     def burn_in(self, fxs, model, graph, n_steps, use_log_amp=False, replay=None, **kwargs):
