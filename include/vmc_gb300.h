@@ -43,7 +43,8 @@ enum vmc_status {
   VMC_ERR_NONFINITE = 3,   /* non-finite amplitude or energy */
   VMC_ERR_SINGULAR = 4,    /* singular orbital matrix */
   VMC_ERR_TIMEOUT = 5,     /* a bounded device-side wait gave up */
-  VMC_ERR_UNSUPPORTED = 6  /* configuration not built into this library */
+  VMC_ERR_UNSUPPORTED = 6, /* configuration not built into this library */
+  VMC_ERR_CAPACITY = 7     /* request larger than a fixed built-in capacity */
 };
 
 int vmc_abi_version(void);
@@ -131,6 +132,21 @@ int vmc_nnbf_local_energy(int prec, const void* const* net_ptrs, int n_sites, in
                           const double* sign, const double* logabs, const int32_t* pairs, const int32_t* offs,
                           int64_t P, int64_t chunk, uint64_t* row_occ, double* coeff, double* term, void* H1, void* H2,
                           void* A, double* eloc, int* d_err, void* stream);
+
+/* Allocation-free variant of vmc_nnbf_eval (mixed precision only, no z0 output).
+ * This entry point has no counterpart in the reference.  It is for callers that
+ * cannot allocate device memory while they run (a fixed device-memory budget
+ * set up once, a real-time loop, or a framework that owns the whole device
+ * pool): it takes no workspace and allocates nothing; its scratch is a fixed
+ * 8.5 MiB array inside the library, held by every GPU that loads the library
+ * until the process exits.  At most 512 configurations per call (nf <= 64);
+ * larger R returns VMC_ERR_CAPACITY.  The first call on each device resolves the
+ * array's device address (cudaGetSymbolAddress) and should come before any
+ * stream capture.  All calls share the one array: calls whose work overlaps on
+ * the GPU (different streams, or different host threads) race on it and must
+ * be serialised by the caller. */
+int vmc_nnbf_eval_noalloc(const void* const* net_ptrs, int n_sites, int nf, int hidden, double bf_scale,
+                          const uint64_t* occ, int64_t R, double* sign, double* logabs, int* d_err, void* stream);
 
 /* ---- minSR in sample space (dtype: 0 = float64, 1 = float32 for O / Oc) ---- */
 int vmc_sr_center(const void* O, int dtype, int64_t Ns, int64_t Np, int64_t ldo, void* Oc, int64_t ldc, double* mean,

@@ -12,8 +12,10 @@ import torch
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libvmc_gb300.so")
 
-VMC_OK, VMC_ERR_ARGS, VMC_ERR_CUDA, VMC_ERR_NONFINITE, VMC_ERR_SINGULAR, VMC_ERR_TIMEOUT, VMC_ERR_UNSUPPORTED = range(7)
+(VMC_OK, VMC_ERR_ARGS, VMC_ERR_CUDA, VMC_ERR_NONFINITE, VMC_ERR_SINGULAR, VMC_ERR_TIMEOUT, VMC_ERR_UNSUPPORTED,
+ VMC_ERR_CAPACITY) = range(8)
 _MSG = {
+    VMC_ERR_CAPACITY: "request exceeds a fixed built-in capacity",
     VMC_ERR_ARGS: "invalid arguments (sizes, null pointers or unsupported shape)",
     VMC_ERR_CUDA: "CUDA launch failed",
     VMC_ERR_NONFINITE: "non-finite amplitude or energy",
@@ -43,6 +45,7 @@ SIGNATURES = {
     "vmc_nnbf_eval": [I32, P, I32, I32, I32, F64, P, I64, P, P, P, P, P, P, P, P],
     "vmc_nnbf_sweep": [I32, P, I32, I32, I32, F64, P, I64, P, I32, I32, F32, U64, U64, P, P, P, P, P, P, P, P, P,
                        P, P, P, P, P, P, P, P],
+    "vmc_nnbf_eval_noalloc": [P, I32, I32, I32, F64, P, I64, P, P, P, P],
     "vmc_nnbf_conn_count": [P, I64, I32, P, I32, P, P],
     "vmc_nnbf_conn_pairs": [P, I64, I32, P, I32, P, P, P],
     "vmc_nnbf_local_energy": [I32, P, I32, I32, I32, F64, P, I64, P, F64, F64, P, P, P, P, P, I64, I64, P, P, P, P,

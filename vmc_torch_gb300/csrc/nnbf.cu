@@ -21,6 +21,7 @@
 // An FP64 twin of every stage (CUDA cores) gives the 1e-10 parity mode.
 #include <cuda_bf16.h>
 #include <utility>
+#include <mutex>
 #include <vector>
 #include <cuda.h>
 #include <cudaTypedefs.h>
@@ -892,7 +893,6 @@ struct StageTimer {
   std::vector<cudaEvent_t> ev;
   std::vector<int> stage;
   size_t used = 0;
-  void begin() {}
   void mark(int stg, bool start) {
     if (!acc) return;
     if (used == ev.size()) {
@@ -1201,3 +1201,71 @@ int vmc_nnbf_local_energy(int prec, const void* const* net_ptrs, int n_sites, in
 }
 
 }  // extern "C"
+
+// ===========================================================================
+// Allocation-free evaluation entry point.
+//
+// Some callers cannot allocate device memory while they run: a host program
+// that drives the evaluation from a region where allocation is forbidden (a
+// fixed device-memory budget set up once at start, a real-time loop, or a
+// framework that owns the whole device pool and rejects foreign allocations).
+// For them this variant of vmc_nnbf_eval (mixed precision only) keeps its
+// scratch -- the two hidden-activation tiles and the per-configuration orbital
+// matrices -- in a fixed array in device memory that is part of this library.
+// Capacity: kNoAllocRows configurations per call with nf <= 64 (8.5 MiB).
+// Every GPU that loads the library holds this array until the process exits.
+// ===========================================================================
+namespace {
+constexpr int64_t kNoAllocRows = 512;
+constexpr size_t kNoAllocH = (size_t)kNoAllocRows * HID * 2;          // one bf16 activation tile, bytes
+constexpr size_t kNoAllocA = (size_t)kNoAllocRows * 64 * 64 * 4;      // orbital matrices, bytes
+static __device__ __align__(256) uint8_t g_noalloc_scratch[2 * kNoAllocH + kNoAllocA];
+
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[64] = {};  // device address of g_noalloc_scratch, per device ordinal
+
+// Host code must not use g_noalloc_scratch as a device address: its host-side
+// name is only a stand-in.  Resolve the real address once per device, with
+// that device current.
+int noalloc_scratch(void** out) {
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return VMC_ERR_CUDA;
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return VMC_ERR_CUDA;
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return VMC_OK;
+}
+}  // namespace
+
+extern "C" int vmc_nnbf_eval_noalloc(const void* const* net_ptrs, int n_sites, int nf, int hidden, double bf_scale,
+                                     const uint64_t* occ, int64_t R, double* sign, double* logabs, int* d_err,
+                                     void* stream) {
+  int st0 = check_shape(0, n_sites, nf, hidden);
+  if (st0) return st0;
+  if (R < 0 || !net_ptrs || !occ || !sign || !logabs || !d_err) return VMC_ERR_ARGS;
+  if (R > kNoAllocRows) return VMC_ERR_CAPACITY;
+  if (R == 0) return VMC_OK;
+  void* scratch = nullptr;
+  int rc = noalloc_scratch(&scratch);
+  if (rc) return rc;
+  set_attrs();
+  cudaStream_t st = (cudaStream_t)stream;
+  // Every scratch row this call reads is written earlier in the same call (rows
+  // beyond R are zero-filled by the TMA bounds check, not read from the array),
+  // so nothing needs clearing between calls.
+  Work wk{scratch, (uint8_t*)scratch + kNoAllocH, (uint8_t*)scratch + 2 * kNoAllocH};
+  NetF32 n32{(const float*)net_ptrs[0], (const float*)net_ptrs[1], (const __nv_bfloat16*)net_ptrs[2],
+             (const float*)net_ptrs[3], (const __nv_bfloat16*)net_ptrs[4], (const float*)net_ptrs[5],
+             (const float*)net_ptrs[6]};
+  const unsigned gw = (unsigned)((R * 32 + 255) / 256);
+  k_prep_fresh<float><<<gw, 256, 0, st>>>(R, n_sites, occ, n32.w0t, n32.b0, nullptr, wk.H1);
+  VMC_CUDA_CHECK_LAUNCH();
+  LdArgs la{};
+  la.sign = sign;
+  la.logabs = logabs;
+  return launch_eval_rows(0, R, n_sites, nf, occ, &n32, bf_scale, wk, d_err, st, LD_EVAL, la);
+}
