@@ -133,6 +133,20 @@ int vmc_nnbf_local_energy(int prec, const void* const* net_ptrs, int n_sites, in
                           int64_t P, int64_t chunk, uint64_t* row_occ, double* coeff, double* term, void* H1, void* H2,
                           void* A, double* eloc, int* d_err, void* stream);
 
+/* Per-sample log-derivatives O = d log|psi| / d theta of the NNBF model
+ * (compute_grads_gpu, vmc_torch/GPU/vmc_utils.py:1389-1634, which the reference
+ * obtains with torch.func.grad): hand-written adjoint, forward activations
+ * recomputed, A^-1 by Gauss-Jordan.  prec 0: FP32, prec 1: FP64 (all arrays of
+ * that type).  gnet[9]: W0^T (2N,256), b0, W1 (256,256), W1^T, b1,
+ * out_w (2N*nf,256), out_w^T (256,2N*nf), out_b, M_base (2N,nf).
+ * Outputs (each nullable): O_full (B, ld_full >= Np) rows in the reference
+ * parameter order; O_dense (B, ld_dense >= Np - 2N*nf*256) the same rows without
+ * the out_w block; kron_g (B, 2N*nf) = s * Gbar and kron_h (B, 256) = h2, whose
+ * outer product is the out_w block; logabs/sign (B). */
+int vmc_nnbf_logpsi_grad(int prec, const void* const* gnet, int n_sites, int nf, int hidden, double bf_scale,
+                         const uint64_t* occ, int64_t B, void* O_full, int64_t ld_full, void* O_dense,
+                         int64_t ld_dense, void* kron_g, void* kron_h, double* logabs, double* sign, void* stream);
+
 /* Allocation-free variant of vmc_nnbf_eval (mixed precision only, no z0 output).
  * This entry point has no counterpart in the reference.  It is for callers that
  * cannot allocate device memory while they run (a fixed device-memory budget

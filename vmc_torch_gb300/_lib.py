@@ -46,6 +46,7 @@ SIGNATURES = {
     "vmc_nnbf_sweep": [I32, P, I32, I32, I32, F64, P, I64, P, I32, I32, F32, U64, U64, P, P, P, P, P, P, P, P, P,
                        P, P, P, P, P, P, P, P],
     "vmc_nnbf_eval_noalloc": [P, I32, I32, I32, F64, P, I64, P, P, P, P],
+    "vmc_nnbf_logpsi_grad": [I32, P, I32, I32, I32, F64, P, I64, P, I64, P, I64, P, P, P, P, P],
     "vmc_nnbf_conn_count": [P, I64, I32, P, I32, P, P],
     "vmc_nnbf_conn_pairs": [P, I64, I32, P, I32, P, P, P],
     "vmc_nnbf_local_energy": [I32, P, I32, I32, I32, F64, P, I64, P, F64, F64, P, P, P, P, P, I64, I64, P, P, P, P,

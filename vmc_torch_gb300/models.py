@@ -361,6 +361,51 @@ class NNBF_GB300(WavefunctionModel_GB300):
             instrument["stage_launches"] = (ctypes.c_int * 4)()
         return (_lib.ptr(instrument["n_eval"]), instrument["stage_ms"], instrument["stage_launches"])
 
+    # ---- per-sample log-derivatives (hand-written adjoint) ----
+    def grad_net(self, device):
+        """Parameters in the adjoint kernel's layout and precision (FP32 for the
+        mixed model, FP64 for the fp64 model)."""
+        key = (self.param_key(), str(device), self.precision, "grad")
+        cache = getattr(self, "_grad_cache", None)
+        if cache is not None and cache[0] == key:
+            return cache[1]
+        dt = torch.float32 if self.precision == "mixed" else torch.float64
+        M_base, w0, b0, w1, b1, out_w, out_b = [q.detach().to(device=device, dtype=dt) for q in self.params]
+        ts = [w0.t().contiguous(), b0.contiguous(), w1.contiguous(), w1.t().contiguous(), b1.contiguous(),
+              out_w.contiguous(), out_w.t().contiguous(), out_b.contiguous(), M_base.contiguous()]
+        arr = (ctypes.c_void_p * 9)(*[t.data_ptr() for t in ts])
+        self._grad_cache = (key, (ts, arr))
+        return ts, arr
+
+    @property
+    def n_params_out_w(self):
+        return self.n_orbitals * self.n_fermions * self.hidden_dim
+
+    def logpsi_grad(self, st, out=None):
+        """(B, Np) O rows in the reference parameter order (FP32 mixed / FP64)."""
+        ts, arr = self.grad_net(st.device)
+        dt = ts[0].dtype
+        if out is None:
+            out = torch.empty((st.B, self.n_params), dtype=dt, device=st.device)
+        _lib.call("vmc_nnbf_logpsi_grad", self._prec, arr, self.n_sites, self.n_fermions, self.hidden_dim,
+                  self.bf_scale, _lib.ptr(st.occ), st.B, _lib.ptr(out), out.stride(0), None, 0, None, None, None,
+                  None, _lib.stream_of(st.device))
+        return out
+
+    def logpsi_grad_factored(self, st):
+        """O in factored form: (O_dense (B, Np - Nw), kron_g (B, 2N*nf), kron_h (B, 256))
+        where the out_w block of row b is kron_g[b] (x) kron_h[b]."""
+        ts, arr = self.grad_net(st.device)
+        dt = ts[0].dtype
+        nd = self.n_params - self.n_params_out_w
+        Od = torch.empty((st.B, nd), dtype=dt, device=st.device)
+        kg = torch.empty((st.B, self.n_orbitals * self.n_fermions), dtype=dt, device=st.device)
+        kh = torch.empty((st.B, self.hidden_dim), dtype=dt, device=st.device)
+        _lib.call("vmc_nnbf_logpsi_grad", self._prec, arr, self.n_sites, self.n_fermions, self.hidden_dim,
+                  self.bf_scale, _lib.ptr(st.occ), st.B, None, 0, _lib.ptr(Od), Od.stride(0), _lib.ptr(kg),
+                  _lib.ptr(kh), None, None, _lib.stream_of(st.device))
+        return Od, kg, kh
+
     def conn_pairs(self, st, H):
         edges = H.edges_on(st.device)
         cnt = torch.empty(st.B, dtype=torch.int32, device=st.device)
