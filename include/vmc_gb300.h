@@ -174,6 +174,19 @@ int vmc_sr_update(const void* Oc, int dtype, int64_t Ns, int64_t Np, int64_t ldc
                   void* stream);
 int vmc_energy_gradient(const void* O, int dtype, int64_t Ns, int64_t Np, int64_t ldo, const double* E, double Ebar,
                         double* g, void* stream);
+/* Factored (Kronecker) SR pieces for the NNBF output layer, whose O block is
+ * g_a (x) h_a per sample (no reference counterpart: the reference materialises
+ * the full O, vmc_torch/GPU/optimizer.py:545-563).
+ * vmc_gemm: C = beta C + alpha op(A) op(B) [* D elementwise], row-major storage,
+ *   ta/tb = 1 transposes A (K x M storage) / B (N x K storage); sk (length K,
+ *   nullable) scales op(A)'s columns; dtype of A, B, sk: 0 f64, 1 f32; C, D f64;
+ *   lower = 1 computes the lower tile triangle of a symmetric result and mirrors it.
+ * vmc_sr_kron_correction: v[a] = P[a] . H[a]; T[a][b] += alpha (mu_sq - v[a] - v[b]). */
+int vmc_gemm(int ta, int tb, int64_t M, int64_t N, int64_t K, double alpha, const void* A, int64_t lda, const void* B,
+             int64_t ldb, const void* sk, int dtype, double beta, double* C, int64_t ldc, const double* D,
+             int64_t ldd, int lower, void* stream);
+int vmc_sr_kron_correction(int64_t n, double* T, int64_t ldt, const double* P, int64_t ldp, const void* H, int dtype,
+                           int64_t ldh, int64_t K, double mu_sq, double alpha, double* v_work, void* stream);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,68 @@
+"""minSR with the Kronecker-factored NNBF output block against the dense
+formulation and the FP64 oracle.  fp64: factored == dense == oracle within
+1e-8 relative (norm); mixed (FP32 O, FP64 Gram accumulation / Cholesky):
+within 2e-3 relative of the FP64 direction."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import lattice, models as om, sr
+import vmc_torch_gb300 as vg
+
+pytestmark = pytest.mark.gpu
+DEV = "cuda"
+
+
+def make(ps, n_sites, nf, precision):
+    m = vg.NNBF_GB300(n_sites, nf, precision=precision).to(DEV)
+    with torch.no_grad():
+        for p, v in zip(m.params, ps):
+            p.copy_(torch.as_tensor(v))
+    m.invalidate()
+    return m
+
+
+def setup(precision, Ns=256, seed=61, N=16, nf=16):
+    ps = om.nnbf_init(N, nf, 256, 2, seed=seed)
+    m = make(ps, N, nf, precision)
+    X = torch.as_tensor(lattice.random_initial_configs(Ns, N, nf // 2, nf // 2, seed=seed + 1), device=DEV)
+    E = torch.as_tensor(np.random.default_rng(seed + 2).standard_normal(Ns) - 3.0, device=DEV)
+    return m, X, E
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+@pytest.mark.parametrize("run_sr", [True, False])
+def test_factored_minsr_equals_dense_and_oracle_fp64(run_sr):
+    m, X, E = setup("fp64")
+    Ns = X.shape[0]
+    O, _ = vg.compute_grads_gpu(X, m, use_log_amp=True)
+    F, _ = vg.compute_grads_factored(X, m)
+    np.testing.assert_allclose(F.full().cpu().numpy(), O.cpu().numpy(), rtol=1e-12, atol=1e-14)
+    kw = dict(local_energies=E, energy_mean=float(E.mean()), total_samples=Ns, n_params=m.n_params,
+              diag_shift=1e-3, device=DEV, run_sr=run_sr)
+    solver = vg.MinSRGB300()
+    dp_d, _, _ = solver.solve(local_o=O, **kw)
+    dp_f, _, _ = solver.solve(local_o=F, **kw)
+    On, En = O.cpu().numpy(), E.cpu().numpy()
+    ref = sr.minsr(On, En, En.mean(), 1e-3) if run_sr else sr.energy_gradient(On, En, En.mean())
+    assert rel(dp_f.cpu().numpy(), ref) < 1e-8
+    assert rel(dp_d.cpu().numpy(), ref) < 1e-8
+
+
+def test_factored_minsr_mixed_precision_vs_fp64():
+    m64, X, E = setup("fp64", N=36, nf=32)   # the mixed forward path needs nf in {32, 64}
+    Ns = X.shape[0]
+    kw = dict(local_energies=E, energy_mean=float(E.mean()), total_samples=Ns, n_params=m64.n_params,
+              diag_shift=1e-3, device=DEV, run_sr=True)
+    F64, _ = vg.compute_grads_factored(X, m64)
+    dp64, _, _ = vg.MinSRGB300().solve(local_o=F64, **kw)
+    m32, _, _ = setup("mixed", N=36, nf=32)
+    F32, _ = vg.compute_grads_factored(X, m32)
+    assert F32.dense.dtype == torch.float32
+    dp32, _, info = vg.MinSRGB300().solve(local_o=F32, **kw)
+    r = rel(dp32.cpu().numpy(), dp64.cpu().numpy())
+    print("mixed factored minSR direction rel err %.2e" % r)
+    assert info == 0 and r < 2e-3

@@ -58,6 +58,8 @@ SIGNATURES = {
     "vmc_sr_rhs": [P, I64, F64, P, P],
     "vmc_sr_update": [P, I32, I64, I64, I64, P, P, P],
     "vmc_energy_gradient": [P, I32, I64, I64, I64, P, F64, P, P],
+    "vmc_gemm": [I32, I32, I64, I64, I64, F64, P, I64, P, I64, P, I32, F64, P, I64, P, I64, I32, P],
+    "vmc_sr_kron_correction": [I64, P, I64, P, I64, P, I32, I64, I64, F64, F64, P, P],
 }
 
 _lib = None

@@ -9,6 +9,44 @@ namespace {
 constexpr int TB = 64;   // output tile
 constexpr int TK = 16;   // k chunk
 
+// FP32 inputs: products are accumulated in FP32 over 4 consecutive k and then
+// folded into a double-float (hi, lo) pair with Knuth's TwoSum, which keeps the
+// Gram matrix accurate to ~FP64 level (its smallest eigenvalues sit at the
+// diagonal shift, ~1e-6 of its norm) at ~2.5x the FP32 cost instead of the
+// 64x of native FP64 arithmetic on GB300.  FP64 inputs accumulate natively.
+template <typename TA>
+struct TileAcc {
+  TA acc[4][4];
+  float lo[4][4];
+  float hi[4][4];
+  __device__ __forceinline__ void zero() {
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+#pragma unroll
+      for (int r = 0; r < 4; ++r) { acc[q][r] = 0; lo[q][r] = 0.f; hi[q][r] = 0.f; }
+  }
+  __device__ __forceinline__ void fold() {
+    if constexpr (sizeof(TA) == 4) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+          const float a = hi[q][r], b = (float)acc[q][r];
+          const float s = a + b;
+          const float bb = s - a;
+          const float err = (a - (s - bb)) + (b - bb);
+          hi[q][r] = s;
+          lo[q][r] += err;
+          acc[q][r] = 0;
+        }
+    }
+  }
+  __device__ __forceinline__ double value(int q, int r) const {
+    if constexpr (sizeof(TA) == 4) return (double)hi[q][r] + (double)lo[q][r] + (double)acc[q][r];
+    return (double)acc[q][r];
+  }
+};
+
 // mean[p] = (1/Ns) sum_i O[i][p];  Oc[i][p] = (O[i][p] - mean[p]) * scale
 template <typename TI, typename TO>
 __global__ void k_center(const TI* __restrict__ O, int64_t Ns, int64_t Np, int64_t ldo, TO* __restrict__ Oc,
@@ -51,7 +89,8 @@ __global__ void k_syrk(const TI* __restrict__ A, int64_t lda, int64_t n, int64_t
   __shared__ TA Bs[TK][TB + 1];
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
   const int64_t i0 = off + (int64_t)bi * TB, j0 = off + (int64_t)bj * TB;
-  TA acc[4][4] = {};
+  TileAcc<TA> T;
+  T.zero();
   for (int64_t k0 = 0; k0 < K; k0 += TK) {
     for (int idx = threadIdx.x; idx < TB * TK; idx += 256) {
       int r = idx / TK, kk = idx - r * TK;
@@ -69,7 +108,8 @@ __global__ void k_syrk(const TI* __restrict__ A, int64_t lda, int64_t n, int64_t
 #pragma unroll
       for (int q = 0; q < 4; ++q)
 #pragma unroll
-        for (int r = 0; r < 4; ++r) acc[q][r] += a[q] * b[r];
+        for (int r = 0; r < 4; ++r) T.acc[q][r] += a[q] * b[r];
+      if ((kk & 3) == 3) T.fold();
     }
     __syncthreads();
   }
@@ -79,7 +119,7 @@ __global__ void k_syrk(const TI* __restrict__ A, int64_t lda, int64_t n, int64_t
     for (int r = 0; r < 4; ++r) {
       int64_t gi = i0 + ty * 4 + q, gj = j0 + tx * 4 + r;
       if (gi < off + n && gj < off + n && gj <= gi) {
-        double v = C[gi * ldc + gj] + sgn * (double)acc[q][r];
+        double v = C[gi * ldc + gj] + sgn * T.value(q, r);
         if (gi == gj) v += diag;
         C[gi * ldc + gj] = v;
         if (mirror && gi != gj) C[gj * ldc + gi] = v;
@@ -287,6 +327,136 @@ int vmc_energy_gradient(const void* O, int dtype, int64_t Ns, int64_t Np, int64_
     k_egrad<float><<<grid, 256, 0, (cudaStream_t)stream>>>((const float*)O, Ns, Np, ldo, E, Ebar, g);
   else
     return VMC_ERR_ARGS;
+  VMC_CUDA_CHECK_LAUNCH();
+  return VMC_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// General GEMM for the factored (Kronecker) SR pieces, CUDA cores:
+//   C = beta * C + alpha * (op(A) op(B)) [elementwise * D]
+// op(A) is M x K (ta = 0: A[m][k] row-major; ta = 1: A[k][m]), op(B) is K x N
+// (tb = 0: B[k][n]; tb = 1: B[n][k]); optional per-k scale s[k] on op(A).
+// Inputs FP32 or FP64 (accumulated in FP64 for FP64 inputs, FP32 per 64x64x16
+// tile step otherwise), C and D FP64.  lower != 0 computes only tiles with
+// tile-row >= tile-col and mirrors them (symmetric results).
+// ---------------------------------------------------------------------------
+namespace {
+template <typename TI, typename TA>
+__global__ void k_gemm_gen(int ta, int tb, int64_t M, int64_t N, int64_t K, double alpha, const TI* __restrict__ A,
+                           int64_t lda, const TI* __restrict__ Bm, int64_t ldb, const TI* __restrict__ sk,
+                           double beta, double* __restrict__ C, int64_t ldc, const double* __restrict__ D,
+                           int64_t ldd, int lower) {
+  const int bi = blockIdx.y, bj = blockIdx.x;
+  if (lower && bj > bi) return;
+  __shared__ TA As[TK][TB + 1];
+  __shared__ TA Bs[TK][TB + 1];
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  const int64_t m0 = (int64_t)bi * TB, n0 = (int64_t)bj * TB;
+  TileAcc<TA> T;
+  T.zero();
+  for (int64_t k0 = 0; k0 < K; k0 += TK) {
+    for (int idx = threadIdx.x; idx < TB * TK; idx += 256) {
+      int r, kk;
+      if (ta) { kk = idx / TB; r = idx - kk * TB; } else { r = idx / TK; kk = idx - r * TK; }
+      const int64_t gm = m0 + r, gk = k0 + kk;
+      TA v = 0;
+      if (gm < M && gk < K) {
+        v = (TA)(ta ? A[gk * lda + gm] : A[gm * lda + gk]);
+        if (sk) v *= (TA)sk[gk];
+      }
+      As[kk][r] = v;
+    }
+    for (int idx = threadIdx.x; idx < TB * TK; idx += 256) {
+      int c, kk;
+      if (tb) { c = idx / TK; kk = idx - c * TK; } else { kk = idx / TB; c = idx - kk * TB; }
+      const int64_t gn = n0 + c, gk = k0 + kk;
+      Bs[kk][c] = (gn < N && gk < K) ? (TA)(tb ? Bm[gn * ldb + gk] : Bm[gk * ldb + gn]) : (TA)0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < TK; ++kk) {
+      TA a[4], b[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) { a[q] = As[kk][ty * 4 + q]; b[q] = Bs[kk][tx * 4 + q]; }
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+#pragma unroll
+        for (int r = 0; r < 4; ++r) T.acc[q][r] += a[q] * b[r];
+      if ((kk & 3) == 3) T.fold();
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int64_t gm = m0 + ty * 4 + q, gn = n0 + tx * 4 + r;
+      if (gm >= M || gn >= N) continue;
+      if (lower && gn > gm) continue;
+      double v = alpha * T.value(q, r);
+      if (D) v *= D[gm * ldd + gn];
+      const double out = (beta == 0.0 ? 0.0 : beta * C[gm * ldc + gn]) + v;
+      C[gm * ldc + gn] = out;
+      if (lower && gm != gn) C[gn * ldc + gm] = out;
+    }
+}
+
+// T[a][b] += alpha * (-v[a] - v[b] + c0)
+__global__ void k_rank_corr(int64_t n, double* __restrict__ T, int64_t ldt, const double* __restrict__ v, double c0,
+                            double alpha) {
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= n * n) return;
+  const int64_t a = idx / n, b = idx - a * n;
+  T[a * ldt + b] += alpha * (c0 - v[a] - v[b]);
+}
+
+// v[a] = sum_k P[a][k] * H[a][k]
+template <typename TI>
+__global__ void k_rowdot(int64_t n, int64_t K, const double* __restrict__ P, int64_t ldp, const TI* __restrict__ H,
+                         int64_t ldh, double* __restrict__ v) {
+  const int64_t a = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (a >= n) return;
+  double s = 0.0;
+  for (int64_t k = lane; k < K; k += 32) s += P[a * ldp + k] * (double)H[a * ldh + k];
+  s = vmc::warp_sum(s);
+  if (lane == 0) v[a] = s;
+}
+}  // namespace
+
+extern "C" {
+
+int vmc_gemm(int ta, int tb, int64_t M, int64_t N, int64_t K, double alpha, const void* A, int64_t lda, const void* B,
+             int64_t ldb, const void* sk, int dtype, double beta, double* C, int64_t ldc, const double* D,
+             int64_t ldd, int lower, void* stream) {
+  if (M <= 0 || N <= 0 || K < 0 || !A || !B || !C || (dtype != 0 && dtype != 1)) return VMC_ERR_ARGS;
+  if (lower && M != N) return VMC_ERR_ARGS;
+  const int64_t mt = (M + TB - 1) / TB, nt = (N + TB - 1) / TB;
+  if (mt > 65535) return VMC_ERR_ARGS;
+  dim3 grid((unsigned)nt, (unsigned)mt);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (dtype == 0)
+    k_gemm_gen<double, double><<<grid, 256, 0, s>>>(ta, tb, M, N, K, alpha, (const double*)A, lda, (const double*)B,
+                                                     ldb, (const double*)sk, beta, C, ldc, D, ldd, lower);
+  else
+    k_gemm_gen<float, float><<<grid, 256, 0, s>>>(ta, tb, M, N, K, alpha, (const float*)A, lda, (const float*)B, ldb,
+                                                   (const float*)sk, beta, C, ldc, D, ldd, lower);
+  VMC_CUDA_CHECK_LAUNCH();
+  return VMC_OK;
+}
+
+int vmc_sr_kron_correction(int64_t n, double* T, int64_t ldt, const double* P, int64_t ldp, const void* H, int dtype,
+                           int64_t ldh, int64_t K, double mu_sq, double alpha, double* v_work, void* stream) {
+  if (n <= 0 || K <= 0 || !T || !P || !H || !v_work || (dtype != 0 && dtype != 1)) return VMC_ERR_ARGS;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (dtype == 0)
+    k_rowdot<double><<<(unsigned)((n + 7) / 8), 256, 0, s>>>(n, K, P, ldp, (const double*)H, ldh, v_work);
+  else
+    k_rowdot<float><<<(unsigned)((n + 7) / 8), 256, 0, s>>>(n, K, P, ldp, (const float*)H, ldh, v_work);
+  const int64_t nn = n * n;
+  k_rank_corr<<<(unsigned)((nn + 255) / 256), 256, 0, s>>>(n, T, ldt, v_work, mu_sq, alpha);
   VMC_CUDA_CHECK_LAUNCH();
   return VMC_OK;
 }

@@ -19,6 +19,18 @@ def evaluate_energy(fxs, model, H, current_amps=None, use_log_amp=False, verbose
     return eloc.mean(), eloc
 
 
+def compute_grads_factored(fxs, model, use_log_amp=True, **kwargs):
+    """Log-derivatives with the NNBF output-layer block in Kronecker-factored
+    form (``optimizer.FactoredO``), for sample-space SR at scale.  Always in log
+    mode: returns (FactoredO, (signs, log_abs))."""
+    from .optimizer import FactoredO
+    with torch.inference_mode():
+        st = model.bind_state(fxs)
+        Od, g, h = model.logpsi_grad_factored(st)
+        off = model.n_params - model.n_params_out_w - model.n_orbitals * model.n_fermions
+        return FactoredO(Od, g, h, off), (st.sign.clone(), st.logabs.clone())
+
+
 def compute_grads_gpu(fxs, model, batch_size=None, verbose=False, offload_to_cpu=False, use_log_amp=False,
                       vectorize=True, vmap_grad=True, bMPS_params_x=None, **kwargs):
     with torch.inference_mode():

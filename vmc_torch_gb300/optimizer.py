@@ -6,9 +6,20 @@ minSR: O~ = (O - <O>)/sqrt(Ns); T = O~ O~^T + lambda I (Ns x Ns, FP64
 accumulation); Cholesky T = L L^T in FP64; x = T^-1 (E - <E>)/sqrt(Ns);
 dp = O~^T x.  The reference solves with torch.linalg.solve and falls back to
 lstsq (info = 1) when that raises; here a non-positive Cholesky pivot triggers
-one retry with the shift raised to 1e-8 * trace(T)/Ns + 10 lambda and info = 1.
+one retry with the shift raised to 10 lambda + 1e-8 trace(T)/Ns and info = 1.
+
+``local_o`` may be a dense (Ns, Np) tensor (the reference's layout) or a
+:class:`FactoredO`, in which the NNBF output-layer block of every row is the
+outer product g_a (x) h_a.  For the factored form the Gram matrix of that block
+is assembled without materialising it:
+
+    (O_k - 1 mu^T)(O_k - 1 mu^T)^T = (G G^T) o (H H^T) - v 1^T - 1 v^T + |mu|^2
+    mu = G^T H / Ns,  v_a = g_a^T mu h_a,
+    dp_k = (G^T diag(x) H - (sum x) mu) / sqrt(Ns),
+
+which reduces the 8x8 NNBF Gram from 2 Ns^2 * 2.2e6 to 2 Ns^2 * (1.15e5 + 8192
++ 256) flops and never stores the 145 GB out_w block of O.
 """
-import math
 import time
 
 import torch
@@ -24,6 +35,56 @@ def _dtype_code(t):
     raise ValueError("O must be float64 or float32")
 
 
+class FactoredO:
+    """Per-sample log-derivatives with one Kronecker-factored block.
+
+    dense: (Ns, Nd) rows of O without the factored block; g: (Ns, Ng);
+    h: (Ns, Nh); the factored block occupies full-parameter indices
+    [offset, offset + Ng*Nh) with row b equal to (g[b][:, None] * h[b][None, :]).ravel().
+    """
+
+    def __init__(self, dense, g, h, offset):
+        self.dense, self.g, self.h, self.offset = dense, g, h, int(offset)
+
+    @property
+    def shape(self):
+        return (self.dense.shape[0], self.n_params)
+
+    @property
+    def n_params(self):
+        return self.dense.shape[1] + self.g.shape[1] * self.h.shape[1]
+
+    @property
+    def device(self):
+        return self.dense.device
+
+    def __getitem__(self, idx):
+        return FactoredO(self.dense[idx], self.g[idx], self.h[idx], self.offset)
+
+    @staticmethod
+    def cat(parts):
+        return FactoredO(torch.cat([p.dense for p in parts]), torch.cat([p.g for p in parts]),
+                         torch.cat([p.h for p in parts]), parts[0].offset)
+
+    def row_norms(self):
+        d = (self.dense.double() ** 2).sum(1)
+        k = (self.g.double() ** 2).sum(1) * (self.h.double() ** 2).sum(1)
+        return (d + k).sqrt()
+
+    def zero_rows(self, mask):
+        self.dense[mask] = 0
+        self.g[mask] = 0
+        self.h[mask] = 0
+
+    def full(self):
+        """Materialise the dense (Ns, Np) matrix (small cases / tests)."""
+        k = (self.g[:, :, None] * self.h[:, None, :]).reshape(self.g.shape[0], -1)
+        return torch.cat([self.dense[:, :self.offset], k, self.dense[:, self.offset:]], dim=1)
+
+    def assemble(self, dp_dense, dp_kron):
+        return torch.cat([dp_dense[:self.offset], dp_kron.reshape(-1), dp_dense[self.offset:]])
+
+
 class PreconditionerGB300:
     def solve(self, *, local_o, local_energies, energy_mean, total_samples, n_params, diag_shift, device, run_sr):
         raise NotImplementedError
@@ -36,11 +97,13 @@ class MinSRGB300(PreconditionerGB300):
               run_sr=True):
         t0 = time.time()
         dev = torch.device(device) if device is not None else torch.device("cuda")
+        E = torch.as_tensor(local_energies, device=dev, dtype=torch.float64).contiguous()
+        if isinstance(local_o, FactoredO):
+            return self._solve_factored(local_o, E, float(energy_mean), n_params, float(diag_shift), dev, run_sr, t0)
         O = torch.as_tensor(local_o, device=dev)
         if O.dtype not in (torch.float64, torch.float32):
             O = O.to(torch.float64)
         O = O.contiguous()
-        E = torch.as_tensor(local_energies, device=dev, dtype=torch.float64).contiguous()
         Ns, Np = O.shape
         if Np != n_params:
             raise ValueError("local_o has %d columns, n_params is %d" % (Np, n_params))
@@ -52,28 +115,88 @@ class MinSRGB300(PreconditionerGB300):
                       _lib.ptr(g), s)
             return g, time.time() - t0, None
         Oc = torch.empty_like(O)
-        mean = torch.empty(Np, dtype=torch.float64, device=dev)
-        _lib.call("vmc_sr_center", _lib.ptr(O), code, Ns, Np, O.stride(0), _lib.ptr(Oc), Oc.stride(0),
-                  _lib.ptr(mean), s)
+        _lib.call("vmc_sr_center", _lib.ptr(O), code, Ns, Np, O.stride(0), _lib.ptr(Oc), Oc.stride(0), None, s)
+
+        def gram(T, shift):
+            _lib.call("vmc_sr_gram", _lib.ptr(Oc), code, Ns, Np, Oc.stride(0), _lib.ptr(T), Ns, shift, 0, s)
+
+        x, info = self._factor_solve(gram, E, float(energy_mean), Ns, float(diag_shift), dev)
+        dp = torch.empty(Np, dtype=torch.float64, device=dev)
+        _lib.call("vmc_sr_update", _lib.ptr(Oc), code, Ns, Np, Oc.stride(0), _lib.ptr(x), _lib.ptr(dp), s)
+        return dp, time.time() - t0, info
+
+    # -- shared: Gram -> (shifted) FP64 Cholesky -> solve --
+    @staticmethod
+    def _factor_solve(build_gram, E, Ebar, Ns, shift, dev):
+        s = _lib.stream_of(dev)
         T = torch.empty((Ns, Ns), dtype=torch.float64, device=dev)
         info = 0
-        shift = float(diag_shift)
         for attempt in range(2):
-            _lib.call("vmc_sr_gram", _lib.ptr(Oc), code, Ns, Np, Oc.stride(0), _lib.ptr(T), Ns, shift, 0, s)
+            build_gram(T, shift)
             flag = torch.zeros(1, dtype=torch.int32, device=dev)
             _lib.call("vmc_sr_cholesky", _lib.ptr(T), Ns, Ns, _lib.ptr(flag), s)
             if int(flag.item()) == 0:
                 break
             info = 1
-            _lib.call("vmc_sr_gram", _lib.ptr(Oc), code, Ns, Np, Oc.stride(0), _lib.ptr(T), Ns, 0.0, 0, s)
+            build_gram(T, 0.0)
             tr = float(torch.diagonal(T).sum().item())
             shift = 10.0 * shift + 1e-8 * tr / Ns
         x = torch.empty(Ns, dtype=torch.float64, device=dev)
-        _lib.call("vmc_sr_rhs", _lib.ptr(E), Ns, float(energy_mean), _lib.ptr(x), s)
+        _lib.call("vmc_sr_rhs", _lib.ptr(E), Ns, Ebar, _lib.ptr(x), s)
         _lib.call("vmc_sr_cholesky_solve", _lib.ptr(T), Ns, Ns, _lib.ptr(x), s)
-        dp = torch.empty(Np, dtype=torch.float64, device=dev)
-        _lib.call("vmc_sr_update", _lib.ptr(Oc), code, Ns, Np, Oc.stride(0), _lib.ptr(x), _lib.ptr(dp), s)
-        return dp, time.time() - t0, info
+        return x, info
+
+    def _solve_factored(self, F, E, Ebar, n_params, shift, dev, run_sr, t0):
+        s = _lib.stream_of(dev)
+        Od, G, H = F.dense.contiguous(), F.g.contiguous(), F.h.contiguous()
+        if not (Od.dtype == G.dtype == H.dtype):
+            raise ValueError("factored O blocks must share one dtype")
+        code = _dtype_code(Od)
+        Ns, Nd = Od.shape
+        Ng, Nh = G.shape[1], H.shape[1]
+        if Nd + Ng * Nh != n_params:
+            raise ValueError("factored O has %d parameters, n_params is %d" % (Nd + Ng * Nh, n_params))
+        # mu = G^T H / Ns  (Ng x Nh, FP64)
+        mu = torch.empty((Ng, Nh), dtype=torch.float64, device=dev)
+        _lib.call("vmc_gemm", 1, 0, Ng, Nh, Ns, 1.0 / Ns, _lib.ptr(G), G.stride(0), _lib.ptr(H), H.stride(0), None,
+                  code, 0.0, _lib.ptr(mu), Nh, None, 0, 0, s)
+        if not run_sr:
+            g = torch.empty(Nd, dtype=torch.float64, device=dev)
+            _lib.call("vmc_energy_gradient", _lib.ptr(Od), code, Ns, Nd, Od.stride(0), _lib.ptr(E), Ebar, _lib.ptr(g), s)
+            # <E O_k> - <E><O_k> = G^T diag(E - Ebar) H / Ns
+            w = (E - Ebar).to(G.dtype).contiguous()
+            gk = torch.empty((Ng, Nh), dtype=torch.float64, device=dev)
+            _lib.call("vmc_gemm", 1, 0, Ng, Nh, Ns, 1.0 / Ns, _lib.ptr(G), G.stride(0), _lib.ptr(H), H.stride(0),
+                      _lib.ptr(w), code, 0.0, _lib.ptr(gk), Nh, None, 0, 0, s)
+            return F.assemble(g, gk), time.time() - t0, None
+        Oc = torch.empty_like(Od)
+        _lib.call("vmc_sr_center", _lib.ptr(Od), code, Ns, Nd, Od.stride(0), _lib.ptr(Oc), Oc.stride(0), None, s)
+        HH = torch.empty((Ns, Ns), dtype=torch.float64, device=dev)
+        _lib.call("vmc_gemm", 0, 1, Ns, Ns, Nh, 1.0, _lib.ptr(H), H.stride(0), _lib.ptr(H), H.stride(0), None, code,
+                  0.0, _lib.ptr(HH), Ns, None, 0, 1, s)
+        mu_c = mu.to(G.dtype).contiguous()
+        P = torch.empty((Ns, Nh), dtype=torch.float64, device=dev)
+        _lib.call("vmc_gemm", 0, 0, Ns, Nh, Ng, 1.0, _lib.ptr(G), G.stride(0), _lib.ptr(mu_c), Nh, None, code, 0.0,
+                  _lib.ptr(P), Nh, None, 0, 0, s)
+        mu_sq = float((mu * mu).sum().item())
+        vwork = torch.empty(Ns, dtype=torch.float64, device=dev)
+
+        def gram(T, sh):
+            _lib.call("vmc_sr_gram", _lib.ptr(Oc), code, Ns, Nd, Oc.stride(0), _lib.ptr(T), Ns, sh, 0, s)
+            _lib.call("vmc_gemm", 0, 1, Ns, Ns, Ng, 1.0 / Ns, _lib.ptr(G), G.stride(0), _lib.ptr(G), G.stride(0),
+                      None, code, 1.0, _lib.ptr(T), Ns, _lib.ptr(HH), Ns, 1, s)
+            _lib.call("vmc_sr_kron_correction", Ns, _lib.ptr(T), Ns, _lib.ptr(P), Nh, _lib.ptr(H), code, H.stride(0),
+                      Nh, mu_sq, 1.0 / Ns, _lib.ptr(vwork), s)
+
+        x, info = self._factor_solve(gram, E, Ebar, Ns, shift, dev)
+        dp_d = torch.empty(Nd, dtype=torch.float64, device=dev)
+        _lib.call("vmc_sr_update", _lib.ptr(Oc), code, Ns, Nd, Oc.stride(0), _lib.ptr(x), _lib.ptr(dp_d), s)
+        rs = Ns ** 0.5
+        dp_k = (-float(x.sum().item()) / rs) * mu
+        xc = x.to(G.dtype).contiguous()
+        _lib.call("vmc_gemm", 1, 0, Ng, Nh, Ns, 1.0 / rs, _lib.ptr(G), G.stride(0), _lib.ptr(H), H.stride(0),
+                  _lib.ptr(xc), code, 1.0, _lib.ptr(dp_k), Nh, None, 0, 0, s)
+        return F.assemble(dp_d, dp_k), time.time() - t0, info
 
 
 class OptimizerGB300:

@@ -14,7 +14,8 @@ from typing import Any, Callable, Dict, Optional
 
 import torch
 
-from .energy import compute_grads_gpu, evaluate_energy
+from .energy import compute_grads_factored, compute_grads_gpu, evaluate_energy
+from .optimizer import FactoredO
 
 
 @dataclass
@@ -33,6 +34,7 @@ class VMCLoopConfig:
     outlier_clip_factor: float = 100.0
     lr_scheduler: object = None
     verbose: bool = False
+    factored_o: bool = False   # NNBF: Kronecker-factored out_w block of O (FactoredO)
 
     def __init__(self, **kwargs):
         for f in fields(self):
@@ -51,7 +53,8 @@ class VMC_GB300:
         self.compute_grads_fn = compute_grads_fn
 
     def _run_sampling_phase(self, fxs, model, hamiltonian, graph, ns_per_rank, grad_batch_size, burn_in=False,
-                            burn_in_steps=0, outlier_clip_factor=0.0, use_log_amp=False, verbose=False):
+                            burn_in_steps=0, outlier_clip_factor=0.0, use_log_amp=False, verbose=False,
+                            factored_o=False):
         B = fxs.shape[0]
         t_samp = t_locE = t_grad = 0.0
         if burn_in and burn_in_steps > 0:
@@ -68,20 +71,26 @@ class VMC_GB300:
             local_E = res[1]
             t_locE += time.time() - t0
             t0 = time.time()
-            grads, aux = self.compute_grads_fn(fxs, model, batch_size=grad_batch_size, use_log_amp=use_log_amp)
-            if not use_log_amp:
-                grads = grads / aux.to(grads.dtype).unsqueeze(1)
+            if factored_o:
+                grads, aux = compute_grads_factored(fxs, model)
+            else:
+                grads, aux = self.compute_grads_fn(fxs, model, batch_size=grad_batch_size, use_log_amp=use_log_amp)
+                if not use_log_amp:
+                    grads = grads / aux.to(grads.dtype).unsqueeze(1)
             t_grad += time.time() - t0
             Es.append(local_E[:need])
             Os.append(grads[:need])
             count += need
         local_E = torch.cat(Es)
-        O = torch.cat(Os)
+        O = FactoredO.cat(Os) if factored_o else torch.cat(Os)
         if outlier_clip_factor > 0:
-            norms = O.norm(dim=1)
+            norms = O.row_norms() if factored_o else O.norm(dim=1)
             keep = norms <= outlier_clip_factor * norms.median()
             if not bool(keep.all()):
-                O[~keep] = 0.0
+                if factored_o:
+                    O.zero_rows(~keep)
+                else:
+                    O[~keep] = 0.0
                 local_E[~keep] = local_E[keep].mean()
         times = {"t_samp": t_samp, "t_locE": t_locE, "t_grad": t_grad}
         return (local_E, O), fxs, t_samp + t_locE + t_grad, times
@@ -102,7 +111,7 @@ class VMC_GB300:
             (E, O), fxs, ts, times = self._run_sampling_phase(
                 fxs, model, hamiltonian, graph, config.ns_per_rank, config.grad_batch_size, burn_in=(step == 0),
                 burn_in_steps=config.burn_in_steps, outlier_clip_factor=config.outlier_clip_factor,
-                use_log_amp=config.use_log_amp, verbose=config.verbose)
+                use_log_amp=config.use_log_amp, verbose=config.verbose, factored_o=config.factored_o)
             n, Em, Evar = self.compute_global_energy_stats(E)
             dp, t_sr, info = self.preconditioner.solve(
                 local_o=O, local_energies=E, energy_mean=Em, total_samples=n, n_params=config.n_params,
