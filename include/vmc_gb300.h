@@ -147,6 +147,41 @@ int vmc_nnbf_logpsi_grad(int prec, const void* const* gnet, int n_sites, int nf,
                          const uint64_t* occ, int64_t B, void* O_full, int64_t ld_full, void* O_dense,
                          int64_t ld_dense, void* kron_g, void* kron_h, double* logabs, double* sign, void* stream);
 
+/* ---- Learned Metropolis-Hastings proposal (no reference counterpart: the
+ * reference samples with local exchange/hop moves only, vmc_torch/GPU/sampler.py:47-137).
+ * Network 2N -> 512 -> 512 -> 256 logits (GELU): logits[0, 2E) one per hop
+ * (edge e of `edges`, index 2e up / 2e+1 down), logits[2E, 2E+4) k = 1..4.
+ * rec: 48-byte record per walker {flag, k, u_acc, logq_fwd, hop[4], logq_rev}. */
+/* wts[6]: W1 (512, Kin) bf16, b1 (512) f32, W2 (512, 512) bf16, b2 f32, Wo (256, 512)
+ * bf16, bo (256) f32; Kin = 2N rounded up to 64.  Workspace X (R, Kin), H1, H2
+ * (R, 512) bf16.  Output logits (R, 256) f32 (tcgen05 BF16 GEMMs). */
+int vmc_prop_logits(const void* const* wts, int n_sites, const uint64_t* occ, int64_t R, void* X, void* H1, void* H2,
+                    float* logits, int* d_err, void* stream);
+/* Draw k and k non-conflicting valid hops per walker; prop_occ, rec (flag, k,
+ * u_acc, hops, log q(x->x') by a DP over the 2^k orderings). */
+int vmc_prop_sample(const int32_t* edges, int n_edges, int n_sites, const float* logits, const uint64_t* occ,
+                    int64_t B, uint64_t seed, uint64_t step, uint64_t* prop_occ, void* rec, void* stream);
+/* log q(x'->x) from the logits at the proposed configurations. */
+int vmc_prop_reverse(const int32_t* edges, int n_edges, int n_sites, const float* logits_p, const uint64_t* prop_occ,
+                     int64_t B, void* rec, void* stream);
+/* MH accept of learned proposals for the mixed NNBF model: psi(x') evaluated
+ * from scratch (z0p workspace), accept with min(1, |psi'/psi|^2 q(x'->x)/q(x->x')). */
+int vmc_nnbf_mh_step(const void* const* net_ptrs, int n_sites, int nf, int hidden, double bf_scale, uint64_t* occ,
+                     int64_t B, const uint64_t* prop_occ, const void* rec4, void* z0, void* z0p, double* sign,
+                     double* logabs, int32_t* n_acc, void* H1, void* H2, void* A, int* d_err, void* stream);
+/* Training (FP32 CUDA cores): forward, masked softmax cross entropy against the
+ * heat-bath hop targets tgt (R, 2E) and the k target ktgt (4), backward, Adam.
+ * params/grad/m1/m2: flat FP32 [W1, b1, W2, b2, Wo, bo]; ws: R*(4*512+2*256) f32;
+ * loss (R) per-row loss; grad holds this step's gradient on return. */
+int vmc_prop_train_step(int n_sites, const int32_t* edges, int n_edges, const uint64_t* occ, int R, const float* Xf,
+                        const float* tgt, const float* ktgt, float kweight, float* params, float* grad, float* m1,
+                        float* m2, int64_t n_params, float lr, float beta1, float beta2, float eps, int t, float* ws,
+                        float* loss, void* stream);
+int vmc_prop_inputs_f32(int n_sites, const uint64_t* occ, int64_t R, float* Xf, void* stream);
+/* tgt[row0 + w][hop] = (term / t)^2 = |psi(x_hop)/psi(x)|^2 from the local-energy pairs. */
+int vmc_prop_collect_targets(const int32_t* pairs, int64_t P, const double* term, double t_abs, int n_hops,
+                             int64_t row0, float* tgt, void* stream);
+
 /* Allocation-free variant of vmc_nnbf_eval (mixed precision only, no z0 output).
  * This entry point has no counterpart in the reference.  It is for callers that
  * cannot allocate device memory while they run (a fixed device-memory budget

@@ -721,7 +721,16 @@ __device__ Det warp_logdet_f64(const double* __restrict__ A, int nf, double* s /
   return d;
 }
 
-enum { LD_ACCEPT = 0, LD_EVAL = 1, LD_ELOC = 2 };
+enum { LD_ACCEPT = 0, LD_EVAL = 1, LD_ELOC = 2, LD_ACCEPT_Q = 3 };
+
+// Learned-proposal record (layout shared with the proposal kernels).
+struct PropRec4 {
+  int flag, k;
+  float u_acc, logq_fwd;
+  int hop[4];
+  float logq_rev;
+  int pad[3];
+};
 
 struct LdArgs {
   // accept
@@ -735,6 +744,9 @@ struct LdArgs {
   double* sign;
   double* logabs;
   unsigned long long* n_eval;  // accept mode: number of proposals evaluated (nullable)
+  // learned-proposal accept
+  const PropRec4* rec4;
+  const void* z0p;             // (B, HID) z0 of the proposed configurations
   // eloc
   const int32_t* pairs;
   const double* coeff;
@@ -751,6 +763,9 @@ __global__ void k_logdet(int64_t R, int64_t row0, int nf, const T* __restrict__ 
   if (MODE == LD_ACCEPT) {
     if (!la.rec[row].flag) return;
     if (la.n_eval && lane == 0) atomicAdd(la.n_eval, 1ull);
+  }
+  if (MODE == LD_ACCEPT_Q) {
+    if (!la.rec4[row].flag) return;
   }
   Det d;
   if constexpr (sizeof(T) == 4) {
@@ -769,6 +784,24 @@ __global__ void k_logdet(int64_t R, int64_t row0, int nf, const T* __restrict__ 
       if (d.sign != 0.0 && la.sign[w] != 0.0) v = la.coeff[row] * d.sign * la.sign[w] * exp(d.logabs - la.logabs[w]);
       la.term[row] = v;
     }
+  } else if (MODE == LD_ACCEPT_Q) {
+    const PropRec4 r = la.rec4[row];
+    // Metropolis-Hastings with the proposal ratio q(x'->x)/q(x->x')
+    const float la2 = (float)(2.0 * (d.logabs - la.logabs[row])) + (r.logq_rev - r.logq_fwd);
+    const float prob = expf(fminf(la2, 80.0f));
+    const bool acc = (d.sign != 0.0) && isfinite(r.logq_rev) && (r.u_acc < prob);
+    if (!acc) return;
+    if (lane == 0) {
+      la.occ[2 * row] = la.prop_occ[2 * row];
+      la.occ[2 * row + 1] = la.prop_occ[2 * row + 1];
+      la.sign[row] = d.sign;
+      la.logabs[row] = d.logabs;
+      la.nacc[row] += 1;
+    }
+    T* z0 = reinterpret_cast<T*>(la.z0);
+    const T* zp = reinterpret_cast<const T*>(la.z0p);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) z0[row * HID + lane * 8 + q] = zp[row * HID + lane * 8 + q];
   } else {
     const PropRec r = la.rec[row];
     // |psi'|^2/|psi|^2 from the FP64 log difference, exponentiated in FP32
@@ -977,10 +1010,12 @@ int launch_eval_rows(int prec, int64_t R, int N, int nf, const uint64_t* row_occ
       if (nf == 64) {
         if (ldmode == LD_ACCEPT) k_logdet<float, 64, LD_ACCEPT><<<gl, 32 * wpb, lsmem, st>>>(Rc, c0, nf, (const float*)wk.A, la);
         else if (ldmode == LD_EVAL) k_logdet<float, 64, LD_EVAL><<<gl, 32 * wpb, lsmem, st>>>(Rc, c0, nf, (const float*)wk.A, la);
+        else if (ldmode == LD_ACCEPT_Q) k_logdet<float, 64, LD_ACCEPT_Q><<<gl, 32 * wpb, lsmem, st>>>(Rc, c0, nf, (const float*)wk.A, la);
         else k_logdet<float, 64, LD_ELOC><<<gl, 32 * wpb, lsmem, st>>>(Rc, c0, nf, (const float*)wk.A, la);
       } else {
         if (ldmode == LD_ACCEPT) k_logdet<float, 32, LD_ACCEPT><<<gl, 32 * wpb, lsmem, st>>>(Rc, c0, nf, (const float*)wk.A, la);
         else if (ldmode == LD_EVAL) k_logdet<float, 32, LD_EVAL><<<gl, 32 * wpb, lsmem, st>>>(Rc, c0, nf, (const float*)wk.A, la);
+        else if (ldmode == LD_ACCEPT_Q) k_logdet<float, 32, LD_ACCEPT_Q><<<gl, 32 * wpb, lsmem, st>>>(Rc, c0, nf, (const float*)wk.A, la);
         else k_logdet<float, 32, LD_ELOC><<<gl, 32 * wpb, lsmem, st>>>(Rc, c0, nf, (const float*)wk.A, la);
       }
       STAGE_END(3);
@@ -1268,4 +1303,38 @@ extern "C" int vmc_nnbf_eval_noalloc(const void* const* net_ptrs, int n_sites, i
   la.sign = sign;
   la.logabs = logabs;
   return launch_eval_rows(0, R, n_sites, nf, occ, &n32, bf_scale, wk, d_err, st, LD_EVAL, la);
+}
+
+// Metropolis-Hastings step with a learned proposal (mixed precision): the
+// proposals (prop_occ, rec4 from vmc_prop_sample / vmc_prop_reverse) are
+// evaluated from scratch and accepted with min(1, |psi'/psi|^2 q(x'->x)/q(x->x')).
+// Workspace: z0p (B, 256) f32, H1/H2/A for B rows.
+extern "C" int vmc_nnbf_mh_step(const void* const* net_ptrs, int n_sites, int nf, int hidden, double bf_scale,
+                                uint64_t* occ, int64_t B, const uint64_t* prop_occ, const void* rec4, void* z0,
+                                void* z0p, double* sign, double* logabs, int32_t* n_acc, void* H1, void* H2, void* A,
+                                int* d_err, void* stream) {
+  int st0 = check_shape(0, n_sites, nf, hidden);
+  if (st0) return st0;
+  if (B < 0 || !net_ptrs || !occ || !prop_occ || !rec4 || !z0 || !z0p || !sign || !logabs || !n_acc || !H1 || !H2 ||
+      !A || !d_err)
+    return VMC_ERR_ARGS;
+  if (B == 0) return VMC_OK;
+  set_attrs();
+  cudaStream_t st = (cudaStream_t)stream;
+  NetF32 n32{(const float*)net_ptrs[0], (const float*)net_ptrs[1], (const __nv_bfloat16*)net_ptrs[2],
+             (const float*)net_ptrs[3], (const __nv_bfloat16*)net_ptrs[4], (const float*)net_ptrs[5],
+             (const float*)net_ptrs[6]};
+  const unsigned gw = (unsigned)((B * 32 + 255) / 256);
+  k_prep_fresh<float><<<gw, 256, 0, st>>>(B, n_sites, prop_occ, n32.w0t, n32.b0, (float*)z0p, H1);
+  VMC_CUDA_CHECK_LAUNCH();
+  LdArgs la{};
+  la.rec4 = (const PropRec4*)rec4;
+  la.prop_occ = prop_occ;
+  la.occ = occ;
+  la.nacc = n_acc;
+  la.z0 = z0;
+  la.z0p = z0p;
+  la.sign = sign;
+  la.logabs = logabs;
+  return launch_eval_rows(0, B, n_sites, nf, prop_occ, &n32, bf_scale, Work{H1, H2, A}, d_err, st, LD_ACCEPT_Q, la);
 }

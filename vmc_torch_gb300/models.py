@@ -434,4 +434,20 @@ class NNBF_GB300(WavefunctionModel_GB300):
                   _lib.ptr(st.sign), _lib.ptr(st.logabs), _lib.ptr(pairs), _lib.ptr(offs), P, chunk,
                   _lib.ptr(row_occ), _lib.ptr(coeff), _lib.ptr(term), _lib.ptr(x["H1"]), _lib.ptr(x["H2"]),
                   _lib.ptr(x["A"]), _lib.ptr(eloc), _lib.ptr(x["err"]), _lib.stream_of(st.device))
+        # kept for the learned proposal: per-hop amplitude ratios of this evaluation
+        self.last_conn = {"pairs": pairs, "P": P, "term": term, "t": float(H.t), "occ": st.occ}
         return eloc
+
+    def mh_step(self, st, prop_occ, rec):
+        """Metropolis-Hastings accept of learned proposals (prop_occ, rec from
+        ``LearnedProposal.propose``)."""
+        if self.precision != "mixed":
+            raise ValueError("the learned-proposal step runs on the mixed-precision model")
+        ts, arr = self.net(st.device)
+        x = st.extra
+        if "z0p" not in x:
+            x["z0p"] = torch.empty_like(x["z0"])
+        _lib.call("vmc_nnbf_mh_step", arr, self.n_sites, self.n_fermions, self.hidden_dim, self.bf_scale,
+                  _lib.ptr(st.occ), st.B, _lib.ptr(prop_occ), _lib.ptr(rec), _lib.ptr(x["z0"]), _lib.ptr(x["z0p"]),
+                  _lib.ptr(st.sign), _lib.ptr(st.logabs), _lib.ptr(st.n_acc), _lib.ptr(x["H1"]), _lib.ptr(x["H2"]),
+                  _lib.ptr(x["A"]), _lib.ptr(x["err"]), _lib.stream_of(st.device))

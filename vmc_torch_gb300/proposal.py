@@ -1,0 +1,208 @@
+"""Learned Metropolis-Hastings proposal and the sampler that uses it.
+
+A small MLP over the occupation bits (2N -> 512 -> 512, GELU) emits one logit
+per nearest-neighbour single-electron hop and four logits for the number k of
+simultaneous hops (1..4).  A proposal draws k, then k mutually non-conflicting
+valid hops without replacement; q(x -> x') sums over the k! draw orders, and the
+reverse probability q(x' -> x) is evaluated with the network at x', so the
+acceptance min(1, |psi'/psi|^2 q(x'->x)/q(x->x')) keeps |psi|^2 exactly
+stationary (libvmc_gb300: vmc_prop_sample / vmc_prop_reverse / vmc_nnbf_mh_step).
+
+Training (hand-written FP32 kernels, vmc_prop_train_step) fits the hop head to
+the heat-bath distribution p(h | x) ~ |psi(x_h)/psi(x)|^2 of the chains' own
+samples -- the ratios the local-energy pass computes anyway -- and the k head to
+the measured accepted-hops-per-proposal of each k.  The last ``buffer`` samples
+are kept in a ring buffer on the device.
+
+No reference counterpart: the reference samples with local exchange / hop moves
+only (vmc_torch/GPU/sampler.py:47-137); plain Metropolis stays available as the
+fallback and as the baseline that judges this proposal (tau_int of E_loc).
+"""
+import math
+
+import torch
+
+from . import _lib
+from .sampler import SamplerGB300
+
+PH, PLOG, KMAX = 512, 256, 4
+
+
+class LearnedProposal:
+    def __init__(self, n_sites, edges, device="cuda", seed=0, lr=1e-3, buffer=65536, kweight=0.1):
+        """edges: int32 (E, 2) device tensor in the Hamiltonian's edge order
+        (hop index 2e + spin matches the local-energy pairs)."""
+        self.N = n_sites
+        self.edges = edges.contiguous()
+        self.E = int(edges.shape[0])
+        self.H = 2 * self.E
+        if self.H + KMAX > PLOG:
+            raise ValueError("too many hops for the logits row (2E + 4 must be <= 256)")
+        self.device = torch.device(device)
+        self.Kin = ((2 * n_sites + 63) // 64) * 64
+        g = torch.Generator().manual_seed(seed)
+        W1 = torch.randn(PH, self.Kin, generator=g) / math.sqrt(2 * n_sites)
+        W1[:, 2 * n_sites:] = 0
+        W2 = torch.randn(PH, PH, generator=g) / math.sqrt(PH)
+        Wo = torch.randn(PLOG, PH, generator=g) * (0.1 / math.sqrt(PH))
+        parts = [W1, torch.zeros(PH), W2, torch.zeros(PH), Wo, torch.zeros(PLOG)]
+        self.params = torch.cat([p.reshape(-1) for p in parts]).to(self.device, torch.float32)
+        self.n_params = self.params.numel()
+        self.grad = torch.zeros_like(self.params)
+        self.m1 = torch.zeros_like(self.params)
+        self.m2 = torch.zeros_like(self.params)
+        self.t = 0
+        self.lr, self.kweight = lr, kweight
+        self.cap = buffer
+        self.buf_occ = torch.zeros((buffer, 2), dtype=torch.int64, device=self.device)
+        self.buf_tgt = torch.zeros((buffer, self.H), dtype=torch.float32, device=self.device)
+        self.n_buf, self.pos = 0, 0
+        self.k_prop = torch.zeros(KMAX, dtype=torch.float64, device=self.device)
+        self.k_acc = torch.zeros(KMAX, dtype=torch.float64, device=self.device)
+        self._wcache = None
+        self._ws = {}
+        self.err = torch.zeros(1, dtype=torch.int32, device=self.device)
+        self.step_counter = 0
+        self.seed = seed
+
+    # ---- views of the flat parameter vector ----
+    def _views(self, v):
+        sizes = [PH * self.Kin, PH, PH * PH, PH, PLOG * PH, PLOG]
+        out, o = [], 0
+        for s in sizes:
+            out.append(v[o:o + s])
+            o += s
+        W1, b1, W2, b2, Wo, bo = out
+        return W1.view(PH, self.Kin), b1, W2.view(PH, PH), b2, Wo.view(PLOG, PH), bo
+
+    def inference_weights(self):
+        if self._wcache is not None and self._wcache[0] == self.t:
+            return self._wcache[1]
+        W1, b1, W2, b2, Wo, bo = self._views(self.params)
+        ts = [W1.to(torch.bfloat16).contiguous(), b1.contiguous(), W2.to(torch.bfloat16).contiguous(),
+              b2.contiguous(), Wo.to(torch.bfloat16).contiguous(), bo.contiguous()]
+        import ctypes
+        arr = (ctypes.c_void_p * 6)(*[t.data_ptr() for t in ts])
+        self._wcache = (self.t, (ts, arr))
+        return ts, arr
+
+    def _work(self, R):
+        if self._ws.get("R", 0) < R:
+            d = self.device
+            self._ws = {"R": R, "X": torch.empty((R, self.Kin), dtype=torch.bfloat16, device=d),
+                        "H1": torch.empty((R, PH), dtype=torch.bfloat16, device=d),
+                        "H2": torch.empty((R, PH), dtype=torch.bfloat16, device=d),
+                        "L": torch.empty((R, PLOG), dtype=torch.float32, device=d),
+                        "L2": torch.empty((R, PLOG), dtype=torch.float32, device=d),
+                        "prop": torch.empty((R, 2), dtype=torch.int64, device=d),
+                        "rec": torch.zeros((R, 12), dtype=torch.int32, device=d)}
+        return self._ws
+
+    def logits(self, occ, out=None):
+        R = occ.shape[0]
+        w = self._work(R)
+        ts, arr = self.inference_weights()
+        L = w["L"][:R] if out is None else out
+        _lib.call("vmc_prop_logits", arr, self.N, _lib.ptr(occ.contiguous()), R, _lib.ptr(w["X"]),
+                  _lib.ptr(w["H1"]), _lib.ptr(w["H2"]), _lib.ptr(L), _lib.ptr(self.err), _lib.stream_of(occ.device))
+        return L
+
+    def propose(self, occ):
+        """Returns (prop_occ (B, 2), rec (B, 12) int32 records) with log q both ways."""
+        B = occ.shape[0]
+        w = self._work(B)
+        s = _lib.stream_of(occ.device)
+        Lx = self.logits(occ, out=w["L"][:B])
+        prop, rec = w["prop"][:B], w["rec"][:B]
+        _lib.call("vmc_prop_sample", _lib.ptr(self.edges), self.E, self.N, _lib.ptr(Lx), _lib.ptr(occ), B,
+                  int(self.seed) & ((1 << 64) - 1), self.step_counter, _lib.ptr(prop), _lib.ptr(rec), s)
+        self.step_counter += 1
+        Lp = self.logits(prop, out=w["L2"][:B])
+        _lib.call("vmc_prop_reverse", _lib.ptr(self.edges), self.E, self.N, _lib.ptr(Lp), _lib.ptr(prop), B,
+                  _lib.ptr(rec), s)
+        return prop, rec
+
+    # ---- data and training ----
+    def record(self, model):
+        """Append the last local-energy evaluation's samples and heat-bath hop
+        targets (|psi(x_h)/psi(x)|^2) to the ring buffer."""
+        lc = getattr(model, "last_conn", None)
+        if lc is None:
+            return
+        occ = lc["occ"]
+        B = occ.shape[0]
+        rows = (self.pos + torch.arange(B, device=self.device)) % self.cap
+        tgt = torch.zeros((B, self.H), dtype=torch.float32, device=self.device)
+        _lib.call("vmc_prop_collect_targets", _lib.ptr(lc["pairs"]), lc["P"], _lib.ptr(lc["term"]), lc["t"], self.H,
+                  0, _lib.ptr(tgt), _lib.stream_of(self.device))
+        self.buf_occ[rows] = occ
+        self.buf_tgt[rows] = tgt
+        self.pos = (self.pos + B) % self.cap
+        self.n_buf = min(self.cap, self.n_buf + B)
+
+    def note_acceptance(self, rec, accepted):
+        k = rec[:, 1].clamp(1, KMAX).long() - 1
+        flag = rec[:, 0] != 0
+        self.k_prop += torch.bincount(k[flag], minlength=KMAX).double()
+        self.k_acc += torch.bincount(k[flag & accepted], minlength=KMAX).double()
+
+    def k_target(self):
+        """p*(k) ~ k * (acceptance rate of k-hop proposals), smoothed."""
+        rate = (self.k_acc + 1.0) / (self.k_prop + 2.0)
+        w = torch.arange(1, KMAX + 1, device=self.device, dtype=torch.float64) * rate
+        return (w / w.sum()).float()
+
+    def train(self, epochs=1, batch=4096, generator=None):
+        n = self.n_buf
+        if n == 0:
+            return None
+        ws_need = batch * (4 * PH + 2 * PLOG)
+        if self._ws.get("train_n", 0) < ws_need:
+            self._ws["train"] = torch.empty(ws_need, dtype=torch.float32, device=self.device)
+            self._ws["train_n"] = ws_need
+            self._ws["Xf"] = torch.empty((batch, self.Kin), dtype=torch.float32, device=self.device)
+            self._ws["loss"] = torch.empty(batch, dtype=torch.float32, device=self.device)
+        kt = self.k_target()
+        s = _lib.stream_of(self.device)
+        losses = []
+        for _ in range(epochs):
+            perm = torch.randperm(n, device=self.device, generator=generator)
+            for b0 in range(0, n - batch + 1 if n >= batch else 1, batch):
+                idx = perm[b0:b0 + batch] if n >= batch else perm
+                R = idx.numel()
+                occ = self.buf_occ[idx].contiguous()
+                tgt = self.buf_tgt[idx].contiguous()
+                Xf = self._ws["Xf"][:R]
+                _lib.call("vmc_prop_inputs_f32", self.N, _lib.ptr(occ), R, _lib.ptr(Xf), s)
+                self.t += 1
+                _lib.call("vmc_prop_train_step", self.N, _lib.ptr(self.edges), self.E, _lib.ptr(occ), R,
+                          _lib.ptr(Xf), _lib.ptr(tgt), _lib.ptr(kt), float(self.kweight), _lib.ptr(self.params),
+                          _lib.ptr(self.grad), _lib.ptr(self.m1), _lib.ptr(self.m2), self.n_params, float(self.lr),
+                          0.9, 0.999, 1e-8, self.t, _lib.ptr(self._ws["train"]), _lib.ptr(self._ws["loss"]), s)
+                losses.append(self._ws["loss"][:R].mean())
+        return float(torch.stack(losses).mean().item()) if losses else None
+
+
+class LearnedSamplerGB300(SamplerGB300):
+    """Metropolis-Hastings sampler with the learned proposal.  One ``step``
+    performs ``moves_per_step`` learned MH moves per walker (the mixed NNBF
+    model evaluates every proposal); it mutates ``fxs`` in place like the
+    reference sampler."""
+
+    def __init__(self, proposal, moves_per_step=112):
+        self.proposal = proposal
+        self.moves_per_step = moves_per_step
+
+    @torch.inference_mode()
+    def step(self, fxs, model, graph=None, use_log_amp=False, **kwargs):
+        st = model.bind_state(fxs)
+        for _ in range(self.moves_per_step):
+            before = st.occ.clone()
+            prop, rec = self.proposal.propose(st.occ)
+            model.mh_step(st, prop, rec)
+            acc = (st.occ == prop).all(1) & (before != prop).any(1)
+            self.proposal.note_acceptance(rec, acc)
+        model.store_configs(st, fxs)
+        if use_log_amp:
+            return fxs, (st.sign.clone(), st.logabs.clone())
+        return fxs, st.sign * torch.exp(st.logabs)
