@@ -155,6 +155,68 @@ def run_reference(args):
 
 
 # ---------------------------------------------------------------------------
+def ess_compare(model, H, fxs, dev, samples=48, moves=28, train_steps=4, epochs=8):
+    """ESS/s of E_loc for plain exchange/hop Metropolis (one 112-edge sweep per
+    sample) vs the learned proposal (``moves`` MH moves per sample), from the
+    same equilibrated walkers at the same parameters.  The proposal is first
+    trained on ``train_steps`` x B plain-chain samples.  ESS/s counts sampler
+    device time (CUDA events); local energies are evaluated after every sample
+    for the estimator and are not part of either sampler's time."""
+    import torch
+    import vmc_torch_gb300 as vg
+    from vmc_torch_gb300.proposal import LearnedProposal, LearnedSamplerGB300
+    from vmc_torch_gb300.stats import split_rhat, tau_int
+
+    graph = H.graph
+    plain = vg.MetropolisExchangeSpinfulSamplerGB300(seed=101)
+    prop = LearnedProposal(LX * LY, H.edges_on(dev), device=dev, seed=5)
+    x = fxs.clone()
+    for _ in range(train_steps):
+        plain.step(x, model, graph)
+        vg.evaluate_energy(x, model, H)
+        prop.record(model)
+    t0 = time.time()
+    loss = None
+    for _ in range(epochs):
+        loss = prop.train(epochs=1, batch=4096)
+    torch.cuda.synchronize()
+    t_train = time.time() - t0
+    learned = LearnedSamplerGB300(prop, moves_per_step=moves)
+
+    def run(sampler, x0):
+        xc = x0.clone()
+        Es, tsum = [], 0.0
+        for _ in range(samples):
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            sampler.step(xc, model, graph)
+            e1.record()
+            torch.cuda.synchronize()
+            tsum += e0.elapsed_time(e1) / 1e3
+            Es.append(vg.evaluate_energy(xc, model, H)[1])
+        E = torch.stack(Es).t().contiguous()
+        tau = tau_int(E)
+        nb = E.shape[0]
+        return {"ess_per_s": nb * samples / tau / tsum, "tau_int_samples": tau, "sampler_s": tsum,
+                "ms_per_sample": 1e3 * tsum / samples, "energy_per_site": float(E.mean().item()) / (LX * LY),
+                "stderr_per_site": float(E.std().item()) / (LX * LY) * (tau / (nb * samples)) ** 0.5,
+                "split_rhat": split_rhat(E)}
+
+    rp = run(plain, x)
+    rl = run(learned, x)
+    acc = float((prop.k_acc.sum() / prop.k_prop.sum().clamp_min(1)).item())
+    dE = abs(rp["energy_per_site"] - rl["energy_per_site"])
+    return {"plain": rp, "learned": rl, "ess_ratio_learned_over_plain": rl["ess_per_s"] / rp["ess_per_s"],
+            "abs_dE_per_site": dE, "matched_energy_1e-3": dE < 1e-3,
+            "dE_sigma": dE / (rp["stderr_per_site"] ** 2 + rl["stderr_per_site"] ** 2) ** 0.5,
+            "samples_per_chain": samples, "learned_moves_per_sample": moves, "learned_acceptance": acc,
+            "proposal_train_loss": loss, "proposal_train_s": t_train,
+            "proposal": "MLP 128->512->512 GELU (BF16 tcgen05 inference, FP32 CUDA-core training), k<=4 hops"}
+
+
+# ---------------------------------------------------------------------------
 def run_gb300(args):
     import torch
     import vmc_torch_gb300 as vg
@@ -283,6 +345,8 @@ def run_gb300(args):
     # n_chunks x (backflow GEMM + LU)) + the unpack of the configurations
     gpu_launches = sum(stage_n) + args.steps * (2 + 2 * n_chunks + 1)
 
+    ess = ess_compare(model, H, fxs, dev) if not args.no_ess else None
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         r, dt, sample = cpu_port_rate(n_walkers=48, n_sweeps=1)
@@ -297,7 +361,8 @@ def run_gb300(args):
                                            float(st.n_acc.float().mean().item()) if st is not None else None,
                                            "evaluated_proposals_per_step": n_eval / args.steps}),
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-                "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": gpu_launches}
+                "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": gpu_launches,
+                "ess": ess}
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
@@ -311,6 +376,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-ess", action="store_true", help="skip the learned-vs-plain ESS/s comparison")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -165,10 +165,14 @@ int vmc_prop_sample(const int32_t* edges, int n_edges, int n_sites, const float*
 int vmc_prop_reverse(const int32_t* edges, int n_edges, int n_sites, const float* logits_p, const uint64_t* prop_occ,
                      int64_t B, void* rec, void* stream);
 /* MH accept of learned proposals for the mixed NNBF model: psi(x') evaluated
- * from scratch (z0p workspace), accept with min(1, |psi'/psi|^2 q(x'->x)/q(x->x')). */
+ * from scratch (z0p workspace), accept with min(1, |psi'/psi|^2 q(x'->x)/q(x->x')).
+ * Optional: lg_x (B, 256) proposal logits at x, overwritten with lg_p's row when a
+ * walker moves (so the next move needs only the logits at its new proposal);
+ * kstats[8] device counters of proposals / acceptances by k. */
 int vmc_nnbf_mh_step(const void* const* net_ptrs, int n_sites, int nf, int hidden, double bf_scale, uint64_t* occ,
                      int64_t B, const uint64_t* prop_occ, const void* rec4, void* z0, void* z0p, double* sign,
-                     double* logabs, int32_t* n_acc, void* H1, void* H2, void* A, int* d_err, void* stream);
+                     double* logabs, int32_t* n_acc, void* H1, void* H2, void* A, float* lg_x, const float* lg_p,
+                     int* kstats, int* d_err, void* stream);
 /* Training (FP32 CUDA cores): forward, masked softmax cross entropy against the
  * heat-bath hop targets tgt (R, 2E) and the k target ktgt (4), backward, Adam.
  * params/grad/m1/m2: flat FP32 [W1, b1, W2, b2, Wo, bo]; ws: R*(4*512+2*256) f32;

@@ -46,7 +46,7 @@ def test_sample_and_reverse_probabilities_match_oracle():
     N, H, prop, X = setup(B=64)
     edges = H.graph.edges()
     occ = vg.pack(torch.as_tensor(X, device=DEV))
-    prop_occ, rec = prop.propose(occ)
+    prop_occ, rec, _ = prop.propose(occ)
     Lx = prop.logits(occ).cpu().numpy()
     Lp = prop.logits(prop_occ).cpu().numpy()
     rec = rec.cpu().numpy()

@@ -747,6 +747,9 @@ struct LdArgs {
   // learned-proposal accept
   const PropRec4* rec4;
   const void* z0p;             // (B, HID) z0 of the proposed configurations
+  float* lg_x;                 // (B, 256) proposal logits at x (nullable): replaced by lg_p on accept
+  const float* lg_p;           // (B, 256) proposal logits at x'
+  int* kstats;                 // [4] proposals and [4] acceptances by k (nullable)
   // eloc
   const int32_t* pairs;
   const double* coeff;
@@ -790,7 +793,16 @@ __global__ void k_logdet(int64_t R, int64_t row0, int nf, const T* __restrict__ 
     const float la2 = (float)(2.0 * (d.logabs - la.logabs[row])) + (r.logq_rev - r.logq_fwd);
     const float prob = expf(fminf(la2, 80.0f));
     const bool acc = (d.sign != 0.0) && isfinite(r.logq_rev) && (r.u_acc < prob);
+    const int kk = min(max(r.k, 1), 4) - 1;
+    if (la.kstats && lane == 0) {
+      atomicAdd(&la.kstats[kk], 1);
+      if (acc) atomicAdd(&la.kstats[4 + kk], 1);
+    }
     if (!acc) return;
+    if (la.lg_x) {  // the walker moved: its proposal logits are now those of x'
+#pragma unroll
+      for (int q = 0; q < 8; ++q) la.lg_x[row * 256 + lane * 8 + q] = la.lg_p[row * 256 + lane * 8 + q];
+    }
     if (lane == 0) {
       la.occ[2 * row] = la.prop_occ[2 * row];
       la.occ[2 * row + 1] = la.prop_occ[2 * row + 1];
@@ -1312,7 +1324,7 @@ extern "C" int vmc_nnbf_eval_noalloc(const void* const* net_ptrs, int n_sites, i
 extern "C" int vmc_nnbf_mh_step(const void* const* net_ptrs, int n_sites, int nf, int hidden, double bf_scale,
                                 uint64_t* occ, int64_t B, const uint64_t* prop_occ, const void* rec4, void* z0,
                                 void* z0p, double* sign, double* logabs, int32_t* n_acc, void* H1, void* H2, void* A,
-                                int* d_err, void* stream) {
+                                float* lg_x, const float* lg_p, int* kstats, int* d_err, void* stream) {
   int st0 = check_shape(0, n_sites, nf, hidden);
   if (st0) return st0;
   if (B < 0 || !net_ptrs || !occ || !prop_occ || !rec4 || !z0 || !z0p || !sign || !logabs || !n_acc || !H1 || !H2 ||
@@ -1336,5 +1348,9 @@ extern "C" int vmc_nnbf_mh_step(const void* const* net_ptrs, int n_sites, int nf
   la.z0p = z0p;
   la.sign = sign;
   la.logabs = logabs;
+  la.lg_x = lg_x;
+  la.lg_p = lg_p;
+  la.kstats = kstats;
+  if ((lg_x != nullptr) != (lg_p != nullptr)) return VMC_ERR_ARGS;
   return launch_eval_rows(0, B, n_sites, nf, prop_occ, &n32, bf_scale, Work{H1, H2, A}, d_err, st, LD_ACCEPT_Q, la);
 }

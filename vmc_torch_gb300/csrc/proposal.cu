@@ -185,49 +185,72 @@ __device__ __forceinline__ void apply_hop(uint64_t& up, uint64_t& dn, const Lat&
   const uint64_t flip = (1ull << i) | (1ull << j);
   if (h & 1) dn ^= flip; else up ^= flip;
 }
-// log P(S | x) over the orders of S (|S| = k <= 4) and log p(k | x).
-// Warp-cooperative: lanes stride over hops.
+// Conflict signature of hop h against the chosen hops S[0..k): bit t is set
+// when h is S[t] or moves the same spin through a site of S[t]'s edge.
+__device__ __forceinline__ unsigned conflict_sig(const Lat& L, int h, const int* S, int k) {
+  unsigned sig = 0;
+#pragma unroll
+  for (int t = 0; t < KMAX; ++t)
+    if (t < k && (h == S[t] || hop_conflict(L, h, S[t]))) sig |= 1u << t;
+  return sig;
+}
+
+__device__ __forceinline__ float warp_max(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(VMC_FULL_MASK, v, o));
+  return v;
+}
+
+// log p(k|x) + log P(S|x), with P(S|x) summed over the k! draw orders by the
+// subset DP.  Z(U) (total weight of hops allowed after drawing the subset U) is
+// accumulated for all 16 subsets in one pass over the hops, each hop adding its
+// weight to the subsets it does not conflict with.  Warp-cooperative.
 __device__ float log_q_set(const float* __restrict__ lg, uint64_t up, uint64_t dn, const Lat& L, const int* S, int k) {
   const int lane = threadIdx.x & 31;
   const int H = 2 * L.E;
-  // stabiliser: max valid logit
   float mx = -INFINITY;
   for (int h = lane; h < H; h += 32)
     if (hop_valid(up, dn, L, h)) mx = fmaxf(mx, lg[h]);
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(VMC_FULL_MASK, mx, o));
+  mx = warp_max(mx);
   if (!(mx > -INFINITY)) return -INFINITY;
-  // Z(U) for every subset U of S
+  const int nU = 1 << k;
   float Z[1 << KMAX];
-  for (int U = 0; U < (1 << k); ++U) {
-    float z = 0.f;
-    for (int h = lane; h < H; h += 32) {
-      if (!hop_valid(up, dn, L, h)) continue;
-      bool excl = false;
-      for (int t = 0; t < k; ++t)
-        if ((U >> t) & 1) excl |= (h == S[t]) || hop_conflict(L, h, S[t]);
-      if (!excl) z += expf(lg[h] - mx);
-    }
-    z = warp_sum(z);
-    Z[U] = z;
+#pragma unroll
+  for (int U = 0; U < (1 << KMAX); ++U) Z[U] = 0.f;
+  for (int h = lane; h < H; h += 32) {
+    if (!hop_valid(up, dn, L, h)) continue;
+    const float wgt = expf(lg[h] - mx);
+    const unsigned sig = conflict_sig(L, h, S, k);
+#pragma unroll
+    for (int U = 0; U < (1 << KMAX); ++U)
+      if (U < nU && !(sig & (unsigned)U)) Z[U] += wgt;
   }
+#pragma unroll
+  for (int U = 0; U < (1 << KMAX); ++U) Z[U] = warp_sum(Z[U]);
+  float e[KMAX];
+#pragma unroll
+  for (int t = 0; t < KMAX; ++t) e[t] = (t < k) ? expf(lg[S[t]] - mx) : 0.f;
   float P[1 << KMAX];
   P[0] = 1.f;
-  for (int T = 1; T < (1 << k); ++T) {
+#pragma unroll
+  for (int T = 1; T < (1 << KMAX); ++T) {
     float p = 0.f;
-    for (int t = 0; t < k; ++t)
+#pragma unroll
+    for (int t = 0; t < KMAX; ++t)
       if ((T >> t) & 1) {
         const int U = T & ~(1 << t);
-        if (Z[U] > 0.f) p += P[U] * expf(lg[S[t]] - mx) / Z[U];
+        if (Z[U] > 0.f) p += P[U] * e[t] / Z[U];
       }
     P[T] = p;
   }
-  // log p(k | x)
+  float pt = 0.f;
+#pragma unroll
+  for (int T = 1; T < (1 << KMAX); ++T)
+    if (T == nU - 1) pt = P[T];
   const float* kl = lg + H;
-  float km = fmaxf(fmaxf(kl[0], kl[1]), fmaxf(kl[2], kl[3]));
-  float kz = expf(kl[0] - km) + expf(kl[1] - km) + expf(kl[2] - km) + expf(kl[3] - km);
+  const float km = fmaxf(fmaxf(kl[0], kl[1]), fmaxf(kl[2], kl[3]));
+  const float kz = expf(kl[0] - km) + expf(kl[1] - km) + expf(kl[2] - km) + expf(kl[3] - km);
   const float lpk = kl[k - 1] - km - logf(kz);
-  const float pt = P[(1 << k) - 1];
   return pt > 0.f ? lpk + logf(pt) : -INFINITY;
 }
 
@@ -240,6 +263,8 @@ struct PropRec4 {
   float logq_rev; // log q(x' -> x), filled by the reverse kernel
   int pad[3];
 };
+
+constexpr int HPL = 8;  // hops per lane (2E <= 252)
 
 // Sample a proposal per walker from logits L(x).
 __global__ void k_prop_sample(int64_t B, Lat L, const float* __restrict__ logits, const uint64_t* __restrict__ occ,
@@ -256,71 +281,82 @@ __global__ void k_prop_sample(int64_t B, Lat L, const float* __restrict__ logits
                         (uint32_t)(seed >> 32));
   const float uk = u24(r0.x), u_acc = u24(r0.y);
   const float uh[4] = {u24(r0.z), u24(r0.w), u24(r1.x), u24(r1.y)};
-  // k
   const float* kl = lg + H;
-  float km = fmaxf(fmaxf(kl[0], kl[1]), fmaxf(kl[2], kl[3]));
+  const float km = fmaxf(fmaxf(kl[0], kl[1]), fmaxf(kl[2], kl[3]));
   float kp[4], kz = 0.f;
+#pragma unroll
   for (int t = 0; t < 4; ++t) { kp[t] = expf(kl[t] - km); kz += kp[t]; }
   int k = 4;
   float acc = 0.f;
-  for (int t = 0; t < 4; ++t) { acc += kp[t] / kz; if (uk < acc) { k = t + 1; break; } }
-  // stabiliser
-  float mx = -INFINITY;
-  for (int h = lane; h < H; h += 32)
-    if (hop_valid(up0, dn0, L, h)) mx = fmaxf(mx, lg[h]);
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(VMC_FULL_MASK, mx, o));
-  int S[4] = {-1, -1, -1, -1};
+  for (int t = 0; t < 4; ++t) {
+    acc += kp[t] / kz;
+    if (k == 4 && uk < acc) k = t + 1;
+  }
+  // per-lane hop weights (lane + 32 q), zero for invalid hops
+  float wv[HPL];
+  bool ex[HPL];
+  float mx = -INFINITY;
+#pragma unroll
+  for (int q = 0; q < HPL; ++q) {
+    const int h = lane + 32 * q;
+    const bool v = h < H && hop_valid(up0, dn0, L, h);
+    wv[q] = v ? lg[h] : -INFINITY;
+    ex[q] = !v;
+    mx = fmaxf(mx, wv[q]);
+  }
+  mx = warp_max(mx);
   bool ok = mx > -INFINITY;
-  for (int t = 0; t < k && ok; ++t) {
-    // total weight of allowed hops
+#pragma unroll
+  for (int q = 0; q < HPL; ++q) wv[q] = ex[q] ? 0.f : expf(wv[q] - mx);
+  int S[4] = {-1, -1, -1, -1};
+#pragma unroll
+  for (int t = 0; t < KMAX; ++t) {
+    if (t >= k || !ok) break;
     float z = 0.f;
-    for (int h = lane; h < H; h += 32) {
-      if (!hop_valid(up0, dn0, L, h)) continue;
-      bool excl = false;
-      for (int q = 0; q < t; ++q) excl |= (h == S[q]) || hop_conflict(L, h, S[q]);
-      if (!excl) z += expf(lg[h] - mx);
-    }
+#pragma unroll
+    for (int q = 0; q < HPL; ++q) z += ex[q] ? 0.f : wv[q];
     z = warp_sum(z);
     if (!(z > 0.f)) { ok = false; break; }
-    // inverse-CDF over hops in index order: chunks of 32, warp prefix sums
     const float target = uh[t] * z;
     float run = 0.f;
     int pick = -1;
-    for (int base = 0; base < H && pick < 0; base += 32) {
-      const int h = base + lane;
-      float wgt = 0.f;
-      if (h < H && hop_valid(up0, dn0, L, h)) {
-        bool excl = false;
-        for (int q = 0; q < t; ++q) excl |= (h == S[q]) || hop_conflict(L, h, S[q]);
-        if (!excl) wgt = expf(lg[h] - mx);
-      }
-      float inc = wgt;
+    // inverse CDF in hop-index order h = 32 q + lane
+#pragma unroll
+    for (int q = 0; q < HPL; ++q) {
+      const float wq = ex[q] ? 0.f : wv[q];
+      float inc = wq;
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
         const float y = __shfl_up_sync(VMC_FULL_MASK, inc, o);
         if (lane >= o) inc += y;
       }
-      const unsigned hit = __ballot_sync(VMC_FULL_MASK, wgt > 0.f && run + inc > target);
-      if (hit) pick = base + __ffs(hit) - 1;
+      const unsigned hit = __ballot_sync(VMC_FULL_MASK, wq > 0.f && run + inc > target);
+      if (pick < 0 && hit) pick = 32 * q + __ffs(hit) - 1;
       run += __shfl_sync(VMC_FULL_MASK, inc, 31);
     }
-    if (pick < 0) {  // rounding at the top end: take the last allowed hop
-      for (int h = H - 1; h >= 0; --h) {
-        if (!hop_valid(up0, dn0, L, h)) continue;
-        bool excl = false;
-        for (int q = 0; q < t; ++q) excl |= (h == S[q]) || hop_conflict(L, h, S[q]);
-        if (!excl) { pick = h; break; }
-      }
+    if (pick < 0) {  // rounding at the top end: the last allowed hop
+      int last = -1;
+#pragma unroll
+      for (int q = 0; q < HPL; ++q)
+        if (!ex[q] && wv[q] > 0.f) last = max(last, lane + 32 * q);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) last = max(last, __shfl_xor_sync(VMC_FULL_MASK, last, o));
+      pick = last;
     }
     S[t] = pick;
+#pragma unroll
+    for (int q = 0; q < HPL; ++q) {
+      const int h = lane + 32 * q;
+      if (h < H && (h == pick || hop_conflict(L, h, pick))) ex[q] = true;
+    }
   }
   PropRec4 rc{};
-  rc.flag = ok ? 1 : 0;
+  rc.flag = (ok && S[k - 1] >= 0) ? 1 : 0;
   rc.k = k;
   rc.u_acc = u_acc;
   uint64_t up = up0, dn = dn0;
-  if (ok) {
+  if (rc.flag) {
     for (int t = 0; t < k; ++t) { rc.hop[t] = S[t]; apply_hop(up, dn, L, S[t]); }
     rc.logq_fwd = log_q_set(lg, up0, dn0, L, S, k);
   }

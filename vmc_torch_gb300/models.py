@@ -438,9 +438,10 @@ class NNBF_GB300(WavefunctionModel_GB300):
         self.last_conn = {"pairs": pairs, "P": P, "term": term, "t": float(H.t), "occ": st.occ}
         return eloc
 
-    def mh_step(self, st, prop_occ, rec):
+    def mh_step(self, st, prop_occ, rec, lg_x=None, lg_p=None, kstats=None):
         """Metropolis-Hastings accept of learned proposals (prop_occ, rec from
-        ``LearnedProposal.propose``)."""
+        ``LearnedProposal.propose``); lg_x rows of moved walkers are replaced by
+        lg_p rows; kstats (8 int32) counts proposals / acceptances by k."""
         if self.precision != "mixed":
             raise ValueError("the learned-proposal step runs on the mixed-precision model")
         ts, arr = self.net(st.device)
@@ -450,4 +451,5 @@ class NNBF_GB300(WavefunctionModel_GB300):
         _lib.call("vmc_nnbf_mh_step", arr, self.n_sites, self.n_fermions, self.hidden_dim, self.bf_scale,
                   _lib.ptr(st.occ), st.B, _lib.ptr(prop_occ), _lib.ptr(rec), _lib.ptr(x["z0"]), _lib.ptr(x["z0p"]),
                   _lib.ptr(st.sign), _lib.ptr(st.logabs), _lib.ptr(st.n_acc), _lib.ptr(x["H1"]), _lib.ptr(x["H2"]),
-                  _lib.ptr(x["A"]), _lib.ptr(x["err"]), _lib.stream_of(st.device))
+                  _lib.ptr(x["A"]), _lib.ptr(lg_x), _lib.ptr(lg_p), _lib.ptr(kstats), _lib.ptr(x["err"]),
+                  _lib.stream_of(st.device))

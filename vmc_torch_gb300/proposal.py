@@ -57,8 +57,8 @@ class LearnedProposal:
         self.buf_occ = torch.zeros((buffer, 2), dtype=torch.int64, device=self.device)
         self.buf_tgt = torch.zeros((buffer, self.H), dtype=torch.float32, device=self.device)
         self.n_buf, self.pos = 0, 0
-        self.k_prop = torch.zeros(KMAX, dtype=torch.float64, device=self.device)
-        self.k_acc = torch.zeros(KMAX, dtype=torch.float64, device=self.device)
+        # device counters: proposals [0:4] and acceptances [4:8] by k
+        self.kstats = torch.zeros(2 * KMAX, dtype=torch.int32, device=self.device)
         self._wcache = None
         self._ws = {}
         self.err = torch.zeros(1, dtype=torch.int32, device=self.device)
@@ -107,12 +107,22 @@ class LearnedProposal:
                   _lib.ptr(w["H1"]), _lib.ptr(w["H2"]), _lib.ptr(L), _lib.ptr(self.err), _lib.stream_of(occ.device))
         return L
 
-    def propose(self, occ):
-        """Returns (prop_occ (B, 2), rec (B, 12) int32 records) with log q both ways."""
+    @property
+    def k_prop(self):
+        return self.kstats[:KMAX].double()
+
+    @property
+    def k_acc(self):
+        return self.kstats[KMAX:].double()
+
+    def propose(self, occ, Lx=None):
+        """Returns (prop_occ (B, 2), rec (B, 12) int32 records, logits at the
+        proposals) with log q both ways.  Lx: logits at occ if already known."""
         B = occ.shape[0]
         w = self._work(B)
         s = _lib.stream_of(occ.device)
-        Lx = self.logits(occ, out=w["L"][:B])
+        if Lx is None:
+            Lx = self.logits(occ, out=w["L"][:B])
         prop, rec = w["prop"][:B], w["rec"][:B]
         _lib.call("vmc_prop_sample", _lib.ptr(self.edges), self.E, self.N, _lib.ptr(Lx), _lib.ptr(occ), B,
                   int(self.seed) & ((1 << 64) - 1), self.step_counter, _lib.ptr(prop), _lib.ptr(rec), s)
@@ -120,7 +130,7 @@ class LearnedProposal:
         Lp = self.logits(prop, out=w["L2"][:B])
         _lib.call("vmc_prop_reverse", _lib.ptr(self.edges), self.E, self.N, _lib.ptr(Lp), _lib.ptr(prop), B,
                   _lib.ptr(rec), s)
-        return prop, rec
+        return prop, rec, Lp
 
     # ---- data and training ----
     def record(self, model):
@@ -139,12 +149,6 @@ class LearnedProposal:
         self.buf_tgt[rows] = tgt
         self.pos = (self.pos + B) % self.cap
         self.n_buf = min(self.cap, self.n_buf + B)
-
-    def note_acceptance(self, rec, accepted):
-        k = rec[:, 1].clamp(1, KMAX).long() - 1
-        flag = rec[:, 0] != 0
-        self.k_prop += torch.bincount(k[flag], minlength=KMAX).double()
-        self.k_acc += torch.bincount(k[flag & accepted], minlength=KMAX).double()
 
     def k_target(self):
         """p*(k) ~ k * (acceptance rate of k-hop proposals), smoothed."""
@@ -196,12 +200,12 @@ class LearnedSamplerGB300(SamplerGB300):
     @torch.inference_mode()
     def step(self, fxs, model, graph=None, use_log_amp=False, **kwargs):
         st = model.bind_state(fxs)
+        P = self.proposal
+        Lx = P.logits(st.occ).clone()   # logits at the current configurations
         for _ in range(self.moves_per_step):
-            before = st.occ.clone()
-            prop, rec = self.proposal.propose(st.occ)
-            model.mh_step(st, prop, rec)
-            acc = (st.occ == prop).all(1) & (before != prop).any(1)
-            self.proposal.note_acceptance(rec, acc)
+            prop, rec, Lp = P.propose(st.occ, Lx)
+            # accepted walkers take x' and its logits (one network evaluation per move)
+            model.mh_step(st, prop, rec, Lx, Lp, P.kstats)
         model.store_configs(st, fxs)
         if use_log_amp:
             return fxs, (st.sign.clone(), st.logabs.clone())
