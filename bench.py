@@ -377,7 +377,10 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-ess", action="store_true", help="skip the learned-vs-plain ESS/s comparison")
+    ap.add_argument("--walkers", type=int, default=B,
+                    help="walkers per GPU (the headline workload uses 16384; smaller values are for profiling)")
     args = ap.parse_args()
+    globals()["B"] = args.walkers
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

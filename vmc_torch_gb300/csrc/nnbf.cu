@@ -565,27 +565,33 @@ struct LuRegs {
   float mant;
   int expo, neg;
   bool ok;
+  unsigned key;  // pivot key of the next step (computed one step ahead)
 };
+
+// Pivot key: max |a| over unretired rows by a single warp reduction on a packed
+// key (|a| bits with the low 6 mantissa bits replaced by 63 - row: larger
+// magnitude wins, ties -> smaller row).  The 6 dropped bits only matter for
+// magnitudes equal to 2^-17 relative, where either choice is a valid pivot.
+template <int NF>
+__device__ __forceinline__ unsigned lu_pivot_key(const LuRegs<NF>& S, int lane) {
+  unsigned key = 0;
+#pragma unroll
+  for (int r = 0; r < NF / 32; ++r) {
+    const int row = lane + 32 * r;
+    if ((S.U >> row) & 1ull) {
+      const unsigned kb = (__float_as_uint(fabsf(S.a[r][0])) & ~63u) | (unsigned)(63 - row);
+      key = kb > key ? kb : key;
+    }
+  }
+  return __reduce_max_sync(VMC_FULL_MASK, key);
+}
 
 template <int NF, int W>
 __device__ __forceinline__ void lu_phase(LuRegs<NF>& S, float* prow, int lane) {
   constexpr int R = NF / 32;
 #pragma unroll 1
   for (int t = 0; t < 16; ++t) {
-    // pivot: max |a| over unretired rows in a single warp reduction on a packed
-    // key (|a| bits with the low 6 mantissa bits replaced by 63 - row: larger
-    // magnitude wins, ties -> smaller row).  The 6 dropped bits only matter for
-    // magnitudes equal to 2^-17 relative, where either choice is a valid pivot.
-    unsigned key = 0;
-#pragma unroll
-    for (int r = 0; r < R; ++r) {
-      const int row = lane + 32 * r;
-      if ((S.U >> row) & 1ull) {
-        const unsigned kb = (__float_as_uint(fabsf(S.a[r][0])) & ~63u) | (unsigned)(63 - row);
-        key = kb > key ? kb : key;
-      }
-    }
-    key = __reduce_max_sync(VMC_FULL_MASK, key);
+    const unsigned key = S.key;
     const int p = 63 - (int)(key & 63u);
     const float best = __uint_as_float(key & ~63u);
     // pivot row -> shared memory (warp-uniform branch on the register row)
@@ -624,11 +630,17 @@ __device__ __forceinline__ void lu_phase(LuRegs<NF>& S, float* prow, int lane) {
       const float4 t4 = reinterpret_cast<const float4*>(prow)[q];
       pr[4 * q] = t4.x; pr[4 * q + 1] = t4.y; pr[4 * q + 2] = t4.z; pr[4 * q + 3] = t4.w;
     }
+    float f[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) {
-      const float f = S.a[r][0] * ipv;   // retired rows keep updating harmlessly
+      f[r] = S.a[r][0] * ipv;   // retired rows keep updating harmlessly
+      S.a[r][0] = fmaf(-f[r], pr[1], S.a[r][1]);   // next pivot column first ...
+    }
+    S.key = lu_pivot_key<NF>(S, lane);             // ... so its reduction overlaps the rest
 #pragma unroll
-      for (int c = 1; c < W; ++c) S.a[r][c - 1] = fmaf(-f, pr[c], S.a[r][c]);
+    for (int r = 0; r < R; ++r) {
+#pragma unroll
+      for (int c = 2; c < W; ++c) S.a[r][c - 1] = fmaf(-f[r], pr[c], S.a[r][c]);
     }
     __syncwarp();
   }
@@ -654,6 +666,7 @@ __device__ __forceinline__ Det warp_logdet_f32(const float* __restrict__ A, floa
   S.expo = 0;
   S.neg = 0;
   S.ok = true;
+  S.key = lu_pivot_key<NF>(S, lane);
   lu_phase<NF, NF>(S, prow, lane);
   lu_phase<NF, NF - 16>(S, prow, lane);
   if constexpr (NF == 64) {
