@@ -26,6 +26,9 @@
  *   vmc_slater_logpsi_grad       — compute_grads_gpu, vmc_torch/GPU/vmc_utils.py:1389-1634
  *   vmc_sr_*                     — minSR_solver_gpu, vmc_torch/GPU/optimizer.py:471-614
  *   vmc_energy_gradient          — the run_sr=False branch, vmc_torch/GPU/optimizer.py:585-613
+ *   vmc_peps_eval / _sweep /     — fPEPS_Model_GPU.amplitude / log_amplitude,
+ *   _local_energy                  vmc_torch/GPU/models/pureTNS.py:82-146, driven by
+ *                                  the same sampler and energy loop as the other models
  */
 #ifndef VMC_GB300_H
 #define VMC_GB300_H
@@ -226,6 +229,43 @@ int vmc_gemm(int ta, int tb, int64_t M, int64_t N, int64_t K, double alpha, cons
              int64_t ldd, int lower, void* stream);
 int vmc_sr_kron_correction(int64_t n, double* T, int64_t ldt, const double* P, int64_t ldp, const void* H, int dtype,
                            int64_t ldh, int64_t K, double mu_sq, double alpha, double* v_work, void* stream);
+
+/* ---- Fermionic PEPS (fPEPS_Model_GPU, vmc_torch/GPU/models/pureTNS.py:24-160) ----
+ * tensors (Lx, Ly, 4, D, D, D, D) = [row][col][quimb state][left][up][right][down],
+ * float32 (prec 0) or float64 (prec 1); Z2-graded (bond parity = index & 1, every
+ * tensor even), open legs at index 0.  Sites i = row * Ly + col.  psi(x) is the
+ * Grassmann contraction with bond variables ordered (left, up, down, right)
+ * within a site, computed exactly (the max_bond -> infinity limit of the
+ * reference's boundary contraction, pureTNS.py:103-114): top and bottom
+ * boundary MPSs of bond D^(Lx/2-1) and a column sweep through the two middle
+ * rows.  Supported: Lx in {4, 6, 8} even, D in {2, 4}, D^(Lx/2-1) <= 16,
+ * Lx * Ly <= 64 (else VMC_ERR_UNSUPPORTED).  Zero amplitudes give sign 0 and
+ * logabs -inf.
+ * vmc_peps_eval         — forward_log of R configurations.
+ * vmc_peps_sweep        — Metropolis sweeps as vmc_slater_sweep (same proposal,
+ *                         random stream and acceptance); n_acc (B, nullable)
+ *                         accumulates accepted moves, d_n_eval (nullable device
+ *                         u64) counts evaluated proposals.
+ * vmc_peps_local_energy — E_loc with pairs/offs from vmc_nnbf_conn_count/pairs;
+ *                         term (P) receives the per-pair hop terms.
+ * vmc_peps_logpsi_grad  — O (B, ldo >= Lx*Ly*4*D^4, dtype of prec) =
+ *                         d log|psi| / d tensors in the flattened tensor order
+ *                         (zero except at each site's occupied state), by a
+ *                         reverse column sweep over stored left environments;
+ *                         work holds work_rows * (Ly+1) * D^(Lx-2) * D^2
+ *                         elements of that dtype; Lx in {4, 6}. */
+int vmc_peps_eval(int prec, const void* tensors, int Lx, int Ly, int D, const uint64_t* occ, int64_t R, double* sign,
+                  double* logabs, void* stream);
+int vmc_peps_sweep(int prec, const void* tensors, int Lx, int Ly, int D, uint64_t* occ, int64_t B,
+                   const int32_t* edges, int n_edges, int n_sweeps, float hopping_rate, uint64_t seed,
+                   uint64_t sweep_offset, const float* r_move, const uint8_t* r_bit, const float* r_acc, double* sign,
+                   double* logabs, int32_t* n_acc, uint64_t* d_n_eval, void* stream);
+int vmc_peps_local_energy(int prec, const void* tensors, int Lx, int Ly, int D, const uint64_t* occ, int64_t B,
+                          const int32_t* edges, double t, double U, const double* sign, const double* logabs,
+                          const int32_t* pairs, const int32_t* offs, int64_t P, double* term, double* eloc,
+                          void* stream);
+int vmc_peps_logpsi_grad(int prec, const void* tensors, int Lx, int Ly, int D, const uint64_t* occ, int64_t B,
+                         void* O, int64_t ldo, void* work, int64_t work_rows, void* stream);
 
 #ifdef __cplusplus
 }

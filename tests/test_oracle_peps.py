@@ -1,0 +1,46 @@
+"""The fPEPS oracle against its own ground truth: the literal Grassmann
+contraction (every bond assignment, sign of the permutation of odd symbols)
+must equal the local sign rule with the plain contraction, the exact
+row-boundary contraction and the boundary contraction at large max_bond."""
+import numpy as np
+import pytest
+
+from oracle import lattice, peps
+
+
+@pytest.mark.parametrize("Lx,Ly,D,nup,ndn,nconf", [(4, 2, 2, 2, 2, 4), (3, 3, 2, 2, 2, 4), (4, 3, 2, 3, 3, 2),
+                                                  (2, 4, 2, 3, 1, 4), (4, 2, 4, 3, 3, 1)])
+def test_sign_rule_matches_grassmann(Lx, Ly, D, nup, ndn, nconf):
+    T = peps.init_tensors(Lx, Ly, D, seed=Lx * 10 + Ly)
+    X = lattice.random_initial_configs(nconf, Lx * Ly, nup, ndn, seed=D)
+    for x in X:
+        g = peps.amp_grassmann(T, x)
+        assert abs(g) > 1e-6
+        np.testing.assert_allclose(peps.amp_bruteforce(T, x), g, rtol=1e-12)
+        if Lx % 2 == 0 and Lx >= 4:
+            np.testing.assert_allclose(peps.amp_rows(T, x), g, rtol=1e-12)
+            np.testing.assert_allclose(peps.amp_boundary_chi(T, x, D ** (Lx // 2)), g, rtol=1e-10)
+
+
+def test_odd_particle_number_vanishes():
+    T = peps.init_tensors(4, 2, 2, seed=0)
+    x = lattice.random_initial_configs(1, 8, 3, 2, seed=0)[0]
+    assert peps.amp_grassmann(T, x) == 0.0
+    assert abs(peps.amp_rows(T, x)) < 1e-14
+
+
+def test_rows_matches_bruteforce_6x4():
+    T = peps.init_tensors(6, 4, 2, seed=5)
+    X = lattice.random_initial_configs(3, 24, 6, 6, seed=6)
+    for x in X:
+        np.testing.assert_allclose(peps.amp_rows(T, x), peps.amp_bruteforce(T, x), rtol=1e-11)
+
+
+def test_truncated_boundary_converges_6x6():
+    """max_bond -> D^(Lx/2) recovers the exact amplitude; max_bond = 16 (the
+    reference's config) is an approximation on random tensors."""
+    T = peps.init_tensors(6, 6, 4, seed=3)
+    x = lattice.random_initial_configs(1, 36, 16, 16, seed=4)[0]
+    ex = peps.amp_rows(T, x)
+    np.testing.assert_allclose(peps.amp_boundary_chi(T, x, 64), ex, rtol=1e-11)
+    assert abs(peps.amp_boundary_chi(T, x, 16) / ex - 1) > 1e-3

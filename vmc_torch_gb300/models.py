@@ -119,6 +119,21 @@ class WavefunctionModel_GB300(nn.Module):
         library replaces with hand-written adjoints)."""
         return self.forward(x.reshape(1, -1))[0]
 
+    def conn_pairs(self, st, H):
+        """(pairs (P, 2) int32 [walker, hop term], offs (B+1) int32, P): every
+        non-zero hop of every walker, term = 2*edge + (0 up, 1 down)."""
+        edges = H.edges_on(st.device)
+        cnt = torch.empty(st.B, dtype=torch.int32, device=st.device)
+        _lib.call("vmc_nnbf_conn_count", _lib.ptr(st.occ), st.B, self.n_sites, _lib.ptr(edges), edges.shape[0],
+                  _lib.ptr(cnt), _lib.stream_of(st.device))
+        offs = torch.zeros(st.B + 1, dtype=torch.int32, device=st.device)
+        offs[1:] = torch.cumsum(cnt, 0)
+        P = int(offs[-1].item())
+        pairs = torch.empty((max(P, 1), 2), dtype=torch.int32, device=st.device)
+        _lib.call("vmc_nnbf_conn_pairs", _lib.ptr(st.occ), st.B, self.n_sites, _lib.ptr(edges), edges.shape[0],
+                  _lib.ptr(offs), _lib.ptr(pairs), _lib.stream_of(st.device))
+        return pairs, offs, P
+
     # ---- hooks implemented by subclasses ----
     def _refresh(self, st, threshold):
         raise NotImplementedError
@@ -406,19 +421,6 @@ class NNBF_GB300(WavefunctionModel_GB300):
                   _lib.ptr(kh), None, None, _lib.stream_of(st.device))
         return Od, kg, kh
 
-    def conn_pairs(self, st, H):
-        edges = H.edges_on(st.device)
-        cnt = torch.empty(st.B, dtype=torch.int32, device=st.device)
-        _lib.call("vmc_nnbf_conn_count", _lib.ptr(st.occ), st.B, self.n_sites, _lib.ptr(edges), edges.shape[0],
-                  _lib.ptr(cnt), _lib.stream_of(st.device))
-        offs = torch.zeros(st.B + 1, dtype=torch.int32, device=st.device)
-        offs[1:] = torch.cumsum(cnt, 0)
-        P = int(offs[-1].item())
-        pairs = torch.empty((max(P, 1), 2), dtype=torch.int32, device=st.device)
-        _lib.call("vmc_nnbf_conn_pairs", _lib.ptr(st.occ), st.B, self.n_sites, _lib.ptr(edges), edges.shape[0],
-                  _lib.ptr(offs), _lib.ptr(pairs), _lib.stream_of(st.device))
-        return pairs, offs, P
-
     def local_energy(self, st, H):
         ts, arr = self.net(st.device)
         edges = H.edges_on(st.device)
@@ -453,3 +455,131 @@ class NNBF_GB300(WavefunctionModel_GB300):
                   _lib.ptr(st.sign), _lib.ptr(st.logabs), _lib.ptr(st.n_acc), _lib.ptr(x["H1"]), _lib.ptr(x["H2"]),
                   _lib.ptr(x["A"]), _lib.ptr(lg_x), _lib.ptr(lg_p), _lib.ptr(kstats), _lib.ptr(x["err"]),
                   _lib.stream_of(st.device))
+
+
+_PEPS_PREC = {"fp32": 0, "fp64": 1}
+
+
+class FPEPS_GB300(WavefunctionModel_GB300):
+    """Fermionic PEPS (fPEPS_Model_GPU, vmc_torch/GPU/models/pureTNS.py:24-160)
+    on an Lx x Ly open square lattice, bond dimension D, physical dimension 4.
+
+    Parameters: one tensor ``(Lx, Ly, 4, D, D, D, D)`` = [row][col][quimb
+    state][left][up][right][down], Z2-graded (bond parity = index & 1, every
+    tensor parity-even, legs leaving the lattice at index 0); the entries
+    outside that structure are zero and stay zero (their log-derivatives are
+    zero).  Sites are numbered ``row * Ly + col`` like the Hamiltonian's.
+
+    The amplitude is the Grassmann contraction of the network (bond variables
+    ordered left, up, down, right within a site), evaluated exactly by the
+    kernels: top/bottom boundary MPSs of bond D^(Lx/2-1) and a column sweep
+    through the two middle rows.  The reference contracts boundary MPSs
+    truncated to ``max_bond`` with SVDs (pureTNS.py:103-114); for
+    ``max_bond >= D**(Lx//2)`` that truncation is exact and the two agree.
+    ``max_bond`` is accepted for interface compatibility; the contraction here
+    is always the exact (max_bond -> infinity) one.
+
+    precision="fp32": FP32 contraction with power-of-two rescaling per column
+    (the production path); "fp64": FP64 (parity mode).
+    Init: entries ~ N(0, init_std^2) (config 5 uses N(0, 1)), masked.
+    """
+
+    def __init__(self, Lx, Ly, D, max_bond=None, dtype=torch.float32, precision="fp32", init_std=1.0,
+                 generator=None, tensors=None):
+        if precision not in _PEPS_PREC:
+            raise ValueError("precision must be 'fp32' or 'fp64'")
+        if Lx % 2 or not 4 <= Lx <= 8 or D not in (2, 4) or D ** (Lx // 2 - 1) > 16 or Lx * Ly > 64:
+            raise ValueError("supported: even Lx in [4, 8], D in {2, 4}, D**(Lx/2-1) <= 16, Lx*Ly <= 64")
+        if tensors is None:
+            tensors = torch.randn((Lx, Ly, 4, D, D, D, D), generator=generator, dtype=torch.float64) * init_std
+        tensors = torch.as_tensor(tensors, dtype=torch.float64).clone()
+        if tuple(tensors.shape) != (Lx, Ly, 4, D, D, D, D):
+            raise ValueError("tensors must have shape (Lx, Ly, 4, D, D, D, D)")
+        tensors = tensors * self.structure_mask(Lx, Ly, D)
+        super().__init__([tensors.to(dtype)], Lx * Ly)
+        self.Lx, self.Ly, self.D = Lx, Ly, D
+        self.max_bond = max_bond
+        self.precision = precision
+        self._cast = None
+
+    @staticmethod
+    def structure_mask(Lx, Ly, D):
+        """(Lx, Ly, 4, D, D, D, D) bool: parity-even entries with open legs at 0."""
+        bp = torch.arange(D) % 2
+        sp = torch.tensor([0, 1, 1, 0])
+        tot = (sp[:, None, None, None, None] + bp[None, :, None, None, None] + bp[None, None, :, None, None]
+               + bp[None, None, None, :, None] + bp[None, None, None, None, :])
+        m = ((tot % 2) == 0).expand(Lx, Ly, 4, D, D, D, D).clone()
+        m[:, 0, :, 1:, :, :, :] = False
+        m[0, :, :, :, 1:, :, :] = False
+        m[:, Ly - 1, :, :, :, 1:, :] = False
+        m[Lx - 1, :, :, :, :, :, 1:] = False
+        return m
+
+    @property
+    def _prec(self):
+        return _PEPS_PREC[self.precision]
+
+    def _tensors(self, device):
+        """Contiguous kernel-dtype copy of the parameters, cached per version."""
+        p = self.params[0]
+        if p.device != device:
+            raise ValueError("model parameters must live on the walkers' device (call model.to(device))")
+        want = torch.float32 if self._prec == 0 else torch.float64
+        key = (self.param_key(), str(device))
+        if self._cast is None or self._cast[0] != key:
+            t = p.detach()
+            t = t if (t.dtype == want and t.is_contiguous()) else t.to(want).contiguous()
+            self._cast = (key, t)
+        return self._cast[1]
+
+    def _shape_args(self):
+        return (self.Lx, self.Ly, self.D)
+
+    def _refresh(self, st, threshold):
+        T = self._tensors(st.device)
+        _lib.call("vmc_peps_eval", self._prec, _lib.ptr(T), *self._shape_args(), _lib.ptr(st.occ), st.B,
+                  _lib.ptr(st.sign), _lib.ptr(st.logabs), _lib.stream_of(st.device))
+
+    def sweep(self, st, graph, n_sweeps, seed, sweep_offset, hopping_rate=0.25, replay=None, n_eval=None):
+        from .hamiltonian import device_sweep_edges
+        T = self._tensors(st.device)
+        edges = device_sweep_edges(graph, st.device)
+        rm = rb = ra = None
+        if replay is not None:
+            rm, rb, ra = replay
+            E = edges.shape[0]
+            for a in (rm, rb, ra):
+                if tuple(a.shape) != (n_sweeps, E, st.B) or not a.is_cuda or not a.is_contiguous():
+                    raise ValueError("replay buffers must be contiguous CUDA tensors of shape (n_sweeps, E, B)")
+        _lib.call("vmc_peps_sweep", self._prec, _lib.ptr(T), *self._shape_args(), _lib.ptr(st.occ), st.B,
+                  _lib.ptr(edges), edges.shape[0], int(n_sweeps), float(hopping_rate), int(seed) & ((1 << 64) - 1),
+                  int(sweep_offset), _lib.ptr(rm), _lib.ptr(rb), _lib.ptr(ra), _lib.ptr(st.sign), _lib.ptr(st.logabs),
+                  _lib.ptr(st.n_acc), _lib.ptr(n_eval), _lib.stream_of(st.device))
+
+    def local_energy(self, st, H):
+        T = self._tensors(st.device)
+        edges = H.edges_on(st.device)
+        pairs, offs, P = self.conn_pairs(st, H)
+        term = torch.empty(max(P, 1), dtype=torch.float64, device=st.device)
+        eloc = torch.empty(st.B, dtype=torch.float64, device=st.device)
+        _lib.call("vmc_peps_local_energy", self._prec, _lib.ptr(T), *self._shape_args(), _lib.ptr(st.occ), st.B,
+                  _lib.ptr(edges), float(H.t), float(H.U), _lib.ptr(st.sign), _lib.ptr(st.logabs), _lib.ptr(pairs),
+                  _lib.ptr(offs), P, _lib.ptr(term), _lib.ptr(eloc), _lib.stream_of(st.device))
+        return eloc
+
+    def logpsi_grad(self, st, out=None, work_rows=None):
+        """O (B, n_params) = d log|psi| / d tensors (flattened parameter order),
+        FP32 for precision "fp32", FP64 for "fp64"; hand-written reverse
+        column sweep (vmc_peps_logpsi_grad)."""
+        T = self._tensors(st.device)
+        dt = torch.float32 if self._prec == 0 else torch.float64
+        if out is None:
+            out = torch.empty((st.B, self.n_params), dtype=dt, device=st.device)
+        da = self.D ** (self.Lx // 2 - 1)
+        esz = da * self.D * self.D * da
+        rows = int(work_rows or min(st.B, 8192))
+        work = torch.empty(rows * (self.Ly + 1) * esz, dtype=dt, device=st.device)
+        _lib.call("vmc_peps_logpsi_grad", self._prec, _lib.ptr(T), *self._shape_args(), _lib.ptr(st.occ), st.B,
+                  _lib.ptr(out), out.stride(0), _lib.ptr(work), rows, _lib.stream_of(st.device))
+        return out
