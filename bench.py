@@ -155,6 +155,97 @@ def run_reference(args):
 
 
 # ---------------------------------------------------------------------------
+PEPS_LX, PEPS_LY, PEPS_D, PEPS_NE, PEPS_B = 6, 6, 4, 16, 8192
+
+
+def peps_flops_per_amp(Lx=PEPS_LX, Ly=PEPS_LY, D=PEPS_D):
+    """Algorithmic FLOP of one exact amplitude: per column and top-bond slice
+    the four contractions of the two-row sweep (D^3 DA^2 + 2 D^5 DA + D^3 DA^2
+    multiply-adds), DA slices, Ly columns, plus the boundary-MPS builds."""
+    da = D ** (Lx // 2 - 1)
+    per_slice = 2 * D ** 3 * da * da + 2 * D ** 5 * da
+    build = 2 * (da * D * da) * D * (Lx // 2 - 2) if Lx > 4 else 0
+    return 2.0 * Ly * (da * per_slice + build)
+
+
+def peps_cpu_rate(n_walkers=6, seed=0):
+    """The oracle's exact contraction driving the CPU port of the sampler on a
+    bounded sample of the 6x6 fPEPS workload."""
+    from oracle import lattice, peps, sampler
+    T = peps.init_tensors(PEPS_LX, PEPS_LY, PEPS_D, seed=seed)
+    edges = lattice.sweep_edges(PEPS_LX, PEPS_LY)
+    X = lattice.random_initial_configs(n_walkers, PEPS_LX * PEPS_LY, PEPS_NE, PEPS_NE, seed=seed + 1)
+    rng = np.random.default_rng(seed + 2)
+    E = len(edges)
+    um = rng.random((1, E, n_walkers), dtype=np.float32)
+    hb = rng.integers(0, 2, (1, E, n_walkers)).astype(np.uint8)
+    ua = rng.random((1, E, n_walkers), dtype=np.float32)
+    t0 = time.perf_counter()
+    sampler.sweep(X, edges, lambda y: peps.logamp(T, y, "rows"), um, hb, ua)
+    dt = time.perf_counter() - t0
+    return n_walkers * E / dt, "%d walkers x 1 sweep x %d edges of the 6x6 D=4 fPEPS (FP64 numpy, exact)" % (
+        n_walkers, E)
+
+
+def peps_block(dev, steps, fp32_peak_tflops, cpu=True):
+    """Secondary workload: 6x6 OBC Hubbard (16+16), fPEPS D=4 with N(0,1) FP32
+    site tensors, 8192 walkers, one Metropolis sweep (60 edges) per step;
+    exact contraction (the max_bond -> infinity limit)."""
+    import torch
+    import vmc_torch_gb300 as vg
+    m = vg.FPEPS_GB300(PEPS_LX, PEPS_LY, PEPS_D, generator=torch.Generator().manual_seed(5)).to(dev)
+    H = vg.spinful_Fermi_Hubbard_square_lattice_torch(PEPS_LX, PEPS_LY, 1.0, 8.0, 2 * PEPS_NE,
+                                                      n_fermions_per_spin=(PEPS_NE, PEPS_NE))
+    H.precompute_hops_gpu(dev)
+    g = H.graph
+    E = len(g.sweep_edges())
+    fx = vg.init_walkers(PEPS_B, PEPS_LX * PEPS_LY, PEPS_NE, PEPS_NE, seed=9, device=dev)
+    smp = vg.MetropolisExchangeSpinfulSamplerGB300(seed=13)
+    smp.burn_in(fx, m, g, 1)
+    st = m.bind_state(fx)
+    ne = torch.zeros(1, dtype=torch.int64, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    ms = 0.0
+    for k in range(steps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        m.sweep(st, g, 1, 13, 100 + k, 0.25, None, n_eval=ne)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms += e0.elapsed_time(e1)
+    n_eval = int(ne.item())
+    fl = peps_flops_per_amp()
+    achieved = n_eval * fl / (ms / 1e3) / 1e12
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    _, eloc = vg.evaluate_energy(fx, m, H)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    el_ms = e0.elapsed_time(e1)
+    e0.record(stream)
+    O = m.logpsi_grad(st)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    gr_ms = e0.elapsed_time(e1)
+    out = {"workload": "6x6 OBC Fermi-Hubbard U=8 (16+16), fPEPS D=4 N(0,1) FP32 tensors, 8192 walkers, "
+                       "exact contraction, one 60-edge Metropolis sweep per step",
+           "value": steps * PEPS_B * E / (ms / 1e3), "unit": UNIT, "ms_per_step": ms / steps,
+           "evaluated_proposals_per_step": n_eval / steps,
+           "roofline": {"bound": "fp32 CUDA-core FMA", "kernel": "k_peps_sweep<float,4,16>", "achieved": achieved,
+                        "peak": fp32_peak_tflops, "unit": "TFLOP/s", "frac": achieved / fp32_peak_tflops,
+                        "algorithmic": "%.4g FLOP per evaluated proposal" % fl,
+                        "peak_source": "nominal: 152 SM x 128 FP32 lanes x 2 x sampled max SM clock"},
+           "local_energy_ms": el_ms, "logpsi_grad_ms": gr_ms, "O_shape": list(O.shape),
+           "energy_per_site": float(eloc.mean().item()) / (PEPS_LX * PEPS_LY)}
+    if cpu:
+        r, sample = peps_cpu_rate()
+        out["cpu_baseline"] = {"value": r, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample}
+    return out
+
+
+# ---------------------------------------------------------------------------
 def ess_compare(model, H, fxs, dev, samples=48, moves=28, train_steps=4, epochs=8):
     """ESS/s of E_loc for plain exchange/hop Metropolis (one 112-edge sweep per
     sample) vs the learned proposal (``moves`` MH moves per sample), from the
@@ -350,6 +441,9 @@ def run_gb300(args):
     gpu_launches = sum(stage_n) + args.steps * (2 + 2 * n_chunks + 1)
 
     ess = ess_compare(model, H, fxs, dev) if not args.no_ess else None
+    smax = clocks.get("sm_max_mhz") or 2070.0
+    peps = peps_block(dev, 2, 152 * 128 * 2 * smax * 1e6 / 1e12, cpu=(rank == 0 and not args.no_cpu_baseline)) \
+        if not args.no_peps else None
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -366,7 +460,7 @@ def run_gb300(args):
                                            "evaluated_proposals_per_step": n_eval / args.steps}),
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
                 "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": gpu_launches,
-                "ess": ess}
+                "ess": ess, "fpeps": peps}
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
@@ -381,14 +475,27 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-ess", action="store_true", help="skip the learned-vs-plain ESS/s comparison")
+    ap.add_argument("--no-peps", action="store_true", help="skip the secondary 6x6 fPEPS workload")
+    ap.add_argument("--peps-only", action="store_true",
+                    help="run only the fPEPS block (print its JSON object); for profiling")
+    ap.add_argument("--peps-walkers", type=int, default=PEPS_B, help="walkers of the fPEPS block (default 8192)")
     ap.add_argument("--walkers", type=int, default=B,
                     help="walkers per GPU (the headline workload uses 16384; smaller values are for profiling)")
     args = ap.parse_args()
     globals()["B"] = args.walkers
     if args.warmup < 3:
         args.warmup = 3
+    globals()["PEPS_B"] = args.peps_walkers
     if args.impl == "reference":
         return run_reference(args)
+    if args.peps_only:
+        import torch
+        from vmc_torch_gb300 import build as vbuild
+        if not os.path.exists(vbuild.LIB):
+            vbuild.build()
+        print(json.dumps(peps_block(torch.device("cuda", 0), args.steps, 152 * 128 * 2 * 2070e6 / 1e12,
+                                    cpu=False)), flush=True)
+        return 0
     return run_gb300(args)
 
 

@@ -20,6 +20,7 @@
 //               energy term / refresh, fused.
 // An FP64 twin of every stage (CUDA cores) gives the 1e-10 parity mode.
 #include <cuda_bf16.h>
+#include <cstdlib>
 #include <utility>
 #include <mutex>
 #include <vector>
@@ -997,6 +998,44 @@ int num_sms() {
 
 void set_attrs();
 
+// Second stream for the chunk pipeline: the backflow GEMM of chunk c+1 runs
+// on it (high priority) while the LU of chunk c runs on the caller's stream;
+// the GEMM is tensor/epilogue work and the LU latency-bound CUDA-core work,
+// so the two share the SMs.  Events order the slot reuse of the two A
+// buffers.  VMC_GB300_SERIAL_CHUNKS=1 runs the chunks back to back instead.
+struct ChunkPipe {
+  int dev = -1;
+  cudaStream_t aux = nullptr;
+  cudaEvent_t h2 = nullptr, g[2] = {nullptr, nullptr}, lu[2] = {nullptr, nullptr};
+  bool ok = false;
+};
+ChunkPipe g_pipe[16];
+std::mutex g_pipe_mu;
+
+ChunkPipe* chunk_pipe() {
+  static const bool serial = [] {
+    const char* e = std::getenv("VMC_GB300_SERIAL_CHUNKS");
+    return e && e[0] == '1';
+  }();
+  if (serial) return nullptr;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 16) return nullptr;
+  std::lock_guard<std::mutex> lk(g_pipe_mu);
+  ChunkPipe& p = g_pipe[dev];
+  if (p.dev == dev) return p.ok ? &p : nullptr;
+  p.dev = dev;
+  int lo = 0, hi = 0;
+  cudaDeviceGetStreamPriorityRange(&lo, &hi);
+  bool ok = cudaStreamCreateWithPriority(&p.aux, cudaStreamNonBlocking, hi) == cudaSuccess;
+  ok = ok && cudaEventCreateWithFlags(&p.h2, cudaEventDisableTiming) == cudaSuccess;
+  for (int i = 0; i < 2; ++i) {
+    ok = ok && cudaEventCreateWithFlags(&p.g[i], cudaEventDisableTiming) == cudaSuccess;
+    ok = ok && cudaEventCreateWithFlags(&p.lu[i], cudaEventDisableTiming) == cudaSuccess;
+  }
+  p.ok = ok;
+  return ok ? &p : nullptr;
+}
+
 int launch_eval_rows(int prec, int64_t R, int N, int nf, const uint64_t* row_occ, const void* net, double scale,
                      const Work& wk, int* err, cudaStream_t st, int ldmode, const LdArgs& la) {
   const int n_orb = 2 * N;
@@ -1015,35 +1054,53 @@ int launch_eval_rows(int prec, int64_t R, int N, int nf, const uint64_t* row_occ
     STAGE_END(1);
     const int n_groups = (n_orb * nf) / TN;
     const int64_t CH = R < kChunkRows ? R : kChunkRows;
+    const int64_t n_chunks = (R + CH - 1) / CH;
     const int wpb = 4;
     const size_t lsmem = wpb * 64 * sizeof(float);
-    for (int64_t c0 = 0; c0 < R; c0 += CH) {
+    // chunk pipeline (two A slots inside the R-row workspace) unless the
+    // stages are being timed one by one
+    ChunkPipe* pipe = (n_chunks > 1 && !g_timer.acc) ? chunk_pipe() : nullptr;
+    if (pipe) {
+      if (cudaEventRecord(pipe->h2, st) != cudaSuccess || cudaStreamWaitEvent(pipe->aux, pipe->h2, 0) != cudaSuccess)
+        return VMC_ERR_CUDA;
+    }
+    for (int64_t ci = 0; ci < n_chunks; ++ci) {
+      const int64_t c0 = ci * CH;
       const int64_t Rc = (R - c0) < CH ? (R - c0) : CH;
+      const int slot = pipe ? (int)(ci & 1) : 0;
+      float* Ac = (float*)wk.A + (size_t)slot * (size_t)CH * nf * nf;
       CUtensorMap tH2c;
       if (!tmap_bf16(&tH2c, (const __nv_bfloat16*)wk.H2 + c0 * HID, (uint64_t)Rc, TM)) return VMC_ERR_UNSUPPORTED;
       PBArgs pa{};
-      pa.row_occ = row_occ + 2 * c0; pa.mbase = n.mbase; pa.outb = n.outb; pa.Aout = (float*)wk.A;
+      pa.row_occ = row_occ + 2 * c0; pa.mbase = n.mbase; pa.outb = n.outb; pa.Aout = Ac;
       pa.scale = (float)scale; pa.n_sites = N; pa.nf = nf; pa.R = (int)Rc;
       pa.n_tiles = (int)((Rc + TM - 1) / TM);
       pa.n_items = n_groups * pa.n_tiles;
       const int grid = pa.n_items < num_sms() ? pa.n_items : num_sms();
+      cudaStream_t gs = pipe ? pipe->aux : st;
+      if (pipe && ci >= 2 && cudaStreamWaitEvent(gs, pipe->lu[slot], 0) != cudaSuccess) return VMC_ERR_CUDA;
       STAGE_BEGIN(2);
-      k_backflow_persistent<<<grid, PB_THREADS, PB_SMEM, st>>>(tH2c, tOW, pa, err);
+      k_backflow_persistent<<<grid, PB_THREADS, PB_SMEM, gs>>>(tH2c, tOW, pa, err);
       STAGE_END(2);
+      if (pipe) {
+        if (cudaEventRecord(pipe->g[slot], gs) != cudaSuccess || cudaStreamWaitEvent(st, pipe->g[slot], 0) != cudaSuccess)
+          return VMC_ERR_CUDA;
+      }
       STAGE_BEGIN(3);
       const unsigned gl = (unsigned)((Rc + wpb - 1) / wpb);
       if (nf == 64) {
-        if (ldmode == LD_ACCEPT) k_logdet<float, 64, LD_ACCEPT><<<gl, 32 * wpb, lsmem, st>>>(Rc, c0, nf, (const float*)wk.A, la);
-        else if (ldmode == LD_EVAL) k_logdet<float, 64, LD_EVAL><<<gl, 32 * wpb, lsmem, st>>>(Rc, c0, nf, (const float*)wk.A, la);
-        else if (ldmode == LD_ACCEPT_Q) k_logdet<float, 64, LD_ACCEPT_Q><<<gl, 32 * wpb, lsmem, st>>>(Rc, c0, nf, (const float*)wk.A, la);
-        else k_logdet<float, 64, LD_ELOC><<<gl, 32 * wpb, lsmem, st>>>(Rc, c0, nf, (const float*)wk.A, la);
+        if (ldmode == LD_ACCEPT) k_logdet<float, 64, LD_ACCEPT><<<gl, 32 * wpb, lsmem, st>>>(Rc, c0, nf, Ac, la);
+        else if (ldmode == LD_EVAL) k_logdet<float, 64, LD_EVAL><<<gl, 32 * wpb, lsmem, st>>>(Rc, c0, nf, Ac, la);
+        else if (ldmode == LD_ACCEPT_Q) k_logdet<float, 64, LD_ACCEPT_Q><<<gl, 32 * wpb, lsmem, st>>>(Rc, c0, nf, Ac, la);
+        else k_logdet<float, 64, LD_ELOC><<<gl, 32 * wpb, lsmem, st>>>(Rc, c0, nf, Ac, la);
       } else {
-        if (ldmode == LD_ACCEPT) k_logdet<float, 32, LD_ACCEPT><<<gl, 32 * wpb, lsmem, st>>>(Rc, c0, nf, (const float*)wk.A, la);
-        else if (ldmode == LD_EVAL) k_logdet<float, 32, LD_EVAL><<<gl, 32 * wpb, lsmem, st>>>(Rc, c0, nf, (const float*)wk.A, la);
-        else if (ldmode == LD_ACCEPT_Q) k_logdet<float, 32, LD_ACCEPT_Q><<<gl, 32 * wpb, lsmem, st>>>(Rc, c0, nf, (const float*)wk.A, la);
-        else k_logdet<float, 32, LD_ELOC><<<gl, 32 * wpb, lsmem, st>>>(Rc, c0, nf, (const float*)wk.A, la);
+        if (ldmode == LD_ACCEPT) k_logdet<float, 32, LD_ACCEPT><<<gl, 32 * wpb, lsmem, st>>>(Rc, c0, nf, Ac, la);
+        else if (ldmode == LD_EVAL) k_logdet<float, 32, LD_EVAL><<<gl, 32 * wpb, lsmem, st>>>(Rc, c0, nf, Ac, la);
+        else if (ldmode == LD_ACCEPT_Q) k_logdet<float, 32, LD_ACCEPT_Q><<<gl, 32 * wpb, lsmem, st>>>(Rc, c0, nf, Ac, la);
+        else k_logdet<float, 32, LD_ELOC><<<gl, 32 * wpb, lsmem, st>>>(Rc, c0, nf, Ac, la);
       }
       STAGE_END(3);
+      if (pipe && cudaEventRecord(pipe->lu[slot], st) != cudaSuccess) return VMC_ERR_CUDA;
     }
   } else {
     const NetF64& n = *(const NetF64*)net;

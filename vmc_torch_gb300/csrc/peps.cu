@@ -45,7 +45,7 @@ struct Peps {
   static constexpr int NT = 32 * NW;
   static constexpr int R = (SL + 31) / 32;     // outputs per lane per step
   static constexpr bool FAST = std::is_same<T, float>::value && D == 4 && DA == 16;  // register-tiled step
-  static constexpr int BUFW = FAST ? 1056 : SL;  // per-warp buffer
+  static constexpr int BUFW = FAST ? 1540 : SL;  // per-warp buffer
   // shared-memory layout (elements of T); the boundary builder's two scratch
   // columns live in the free environment buffer (ESZ >= 2 MSZ)
   static constexpr size_t off_M = 0, off_N = off_M + MSZ, off_E0 = off_N + MSZ, off_E1 = off_E0 + ESZ,
@@ -70,7 +70,8 @@ __device__ __forceinline__ int exp2_of<double>(double m) { return ilogb(m); }
 // to 0.  top = true: M[a][d][b] from row 0 down; false: N[a][u][b] from row
 // Lx-1 up.  ping/pong are scratch of MSZ each.  CTA-wide, ends synchronised.
 template <typename T, int D, int DA>
-__device__ void build_boundary(const T* tcol, int Lx, bool top, T* dst, T* ping, T* pong, T scale) {
+__device__ void build_boundary(const T* tcol, int Lx, bool top, T* dst, T* ping, T* pong, T scale,
+                               bool transposed = false) {
   using P = Peps<T, D, DA>;
   const int nr = Lx / 2 - 1;
   const int r0 = top ? 0 : Lx - 1;
@@ -82,7 +83,8 @@ __device__ void build_boundary(const T* tcol, int Lx, bool top, T* dst, T* ping,
       const int l = o / (D * D), v = (o / D) % D, r = o % D;
       // top: A[l][0][r][v]; bottom: A[l][v][r][0]
       const T val = top ? A[((l * D + 0) * D + r) * D + v] : A[((l * D + v) * D + r) * D + 0];
-      cur[o] = (nr == 1) ? val * scale : val;
+      if (nr == 1) dst[transposed ? (r * D + l) * D + v : o] = val * scale;
+      else cur[o] = val;
     }
   }
   __syncthreads();
@@ -92,8 +94,11 @@ __device__ void build_boundary(const T* tcol, int Lx, bool top, T* dst, T* ping,
     const T* A = tcol + (size_t)rr * P::D4;
     T* nxt = (k == nr - 1) ? dst : (cur == ping ? pong : ping);
     const int dn = da * D;
+    const bool tr = transposed && k == nr - 1;  // walk the destination order: conflict-free stores
     for (int o = threadIdx.x; o < dn * D * dn; o += blockDim.x) {
-      const int an = o / (D * dn), v2 = (o / dn) % D, bn = o % dn;
+      const int an = tr ? (o / D) % dn : o / (D * dn);
+      const int v2 = tr ? o % D : (o / dn) % D;
+      const int bn = tr ? o / (D * dn) : o % dn;
       const int a = an / D, l = an % D, b = bn / D, r = bn % D;
       T acc = 0;
 #pragma unroll
@@ -102,7 +107,8 @@ __device__ void build_boundary(const T* tcol, int Lx, bool top, T* dst, T* ping,
         const T av = top ? A[((l * D + v) * D + r) * D + v2] : A[((l * D + v2) * D + r) * D + v];
         acc += cur[(a * D + v) * da + b] * av;
       }
-      nxt[o] = (k == nr - 1) ? acc * scale : acc;
+      if (k == nr - 1) dst[o] = acc * scale;
+      else nxt[o] = acc;
     }
     __syncthreads();
     cur = nxt;
@@ -196,11 +202,13 @@ struct SliceStep {
 // (l2, u2) contraction is lane-local; the (l3, d2) contraction takes the other
 // two l3 values from lane ^ 16 (16 shuffles) with lane h keeping
 // r2 in {2h, 2h+1}; the (d3, a') contraction goes through the warp's buffer
-// (X3 stored [h][d3][a'][r2 r3], halves 528 floats apart so that their
-// broadcast reads fall in different banks).
+// (X3 stored [h][d3][a'][r2 r3] with 12-float rows, so that 8 consecutive
+// lanes' 16-byte stores hit distinct bank groups, and the halves 772 floats
+// apart, so that their broadcast reads do too).  M arrives transposed,
+// [b][a][u2], for one 16-byte load per a.
 template <>
 struct SliceStep<float, 4, 16> {
-  static constexpr int HALF = 528;
+  static constexpr int HALF = 772;
   static __device__ __forceinline__ float run(const float* __restrict__ Mc, const float* __restrict__ E0,
                                               const float* __restrict__ A2, const float* __restrict__ A3,
                                               const float* __restrict__ Nc, float* __restrict__ buf,
@@ -214,9 +222,8 @@ struct SliceStep<float, 4, 16> {
       for (int l = 0; l < 4; ++l) y[u][l][0] = y[u][l][1] = 0.f;
 #pragma unroll 2
     for (int a = 0; a < 16; ++a) {
-      float m[4];
-#pragma unroll
-      for (int u = 0; u < 4; ++u) m[u] = Mc[(a * 4 + u) * 16 + b];
+      const float4 m4 = *reinterpret_cast<const float4*>(Mc + (b * 16 + a) * 4);  // M stored [b][a][u2]
+      const float m[4] = {m4.x, m4.y, m4.z, m4.w};
       const float* e = E0 + a * 256 + h * 16 + ap;
 #pragma unroll
       for (int l = 0; l < 4; ++l)
@@ -284,11 +291,11 @@ struct SliceStep<float, 4, 16> {
             x3[rr][r][3] = fmaf(ao.w, vo, fmaf(aq.w, vp, x3[rr][r][3]));
           }
         }
-    // ---- stage X3 as [h][d3][a'][rr*4 + r3] ----
+    // ---- stage X3 as [h][d3][a'][rr*4 + r3], rows padded to 12 floats ----
     float* xb = buf + h * HALF;
 #pragma unroll
     for (int d3 = 0; d3 < 4; ++d3) {
-      float4* dst = reinterpret_cast<float4*>(xb + (d3 * 16 + ap) * 8);
+      float4* dst = reinterpret_cast<float4*>(xb + (d3 * 16 + ap) * 12);
       dst[0] = make_float4(x3[0][0][d3], x3[0][1][d3], x3[0][2][d3], x3[0][3][d3]);
       dst[1] = make_float4(x3[1][0][d3], x3[1][1][d3], x3[1][2][d3], x3[1][3][d3]);
     }
@@ -301,8 +308,8 @@ struct SliceStep<float, 4, 16> {
     for (int q = 0; q < 64; ++q) {  // q = d3 * 16 + a'
       const int d3 = q >> 4, a2 = q & 15;
       const float n = Nc[(a2 * 4 + d3) * 16 + ap];
-      const float4 v0 = *reinterpret_cast<const float4*>(xb + q * 8);
-      const float4 v1 = *reinterpret_cast<const float4*>(xb + q * 8 + 4);
+      const float4 v0 = *reinterpret_cast<const float4*>(xb + q * 12);
+      const float4 v1 = *reinterpret_cast<const float4*>(xb + q * 12 + 4);
       acc[0] = fmaf(v0.x, n, acc[0]); acc[1] = fmaf(v0.y, n, acc[1]);
       acc[2] = fmaf(v0.z, n, acc[2]); acc[3] = fmaf(v0.w, n, acc[3]);
       acc[4] = fmaf(v1.x, n, acc[4]); acc[5] = fmaf(v1.y, n, acc[5]);
@@ -310,9 +317,10 @@ struct SliceStep<float, 4, 16> {
     }
     float wmax = 0.f;
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {  // k = rr * 4 + r3 -> (r2 * 4 + r3) = 8h + k
-      E1[b * 256 + (8 * h + k) * 16 + ap] = acc[k];
-      wmax = fmaxf(wmax, fabsf(acc[k]));
+    for (int k = 0; k < 8; ++k) {  // row (r2 * 4 + r3) = 8h + (k ^ h): the halves hit different banks
+      const float v = h ? acc[k ^ 1] : acc[k];
+      E1[b * 256 + (8 * h + (k ^ h)) * 16 + ap] = v;
+      wmax = fmaxf(wmax, fabsf(v));
     }
     __syncwarp();
     return wmax;
@@ -358,7 +366,7 @@ __device__ void peps_amp(const T* __restrict__ tens, int Lx, int Ly, uint64_t up
     }
     __syncthreads();
     // E1 (the free environment buffer) doubles as the builder's scratch
-    build_boundary<T, D, DA>(tcol, Lx, true, Mc, E1, E1 + P::MSZ, scale);
+    build_boundary<T, D, DA>(tcol, Lx, true, Mc, E1, E1 + P::MSZ, scale, P::FAST);
     build_boundary<T, D, DA>(tcol, Lx, false, Nc, E1, E1 + P::MSZ, T(1));
     // ---- per-slice sweep step ----
     T wmax = 0;
