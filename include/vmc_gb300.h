@@ -245,9 +245,18 @@ int vmc_sr_kron_correction(int64_t n, double* T, int64_t ldt, const double* P, i
  * vmc_peps_sweep        — Metropolis sweeps as vmc_slater_sweep (same proposal,
  *                         random stream and acceptance); n_acc (B, nullable)
  *                         accumulates accepted moves, d_n_eval (nullable device
- *                         u64) counts evaluated proposals.
+ *                         u64[2]) accumulates evaluated proposals and column
+ *                         steps executed.
  * vmc_peps_local_energy — E_loc with pairs/offs from vmc_nnbf_conn_count/pairs;
- *                         term (P) receives the per-pair hop terms.
+ *                         term (P, nullable with env_work) receives the
+ *                         per-pair hop terms.
+ *   env_work (nullable): work_rows * 2 * (Ly+1) * D^(Lx-2) * D^2 elements of the
+ *   tensors' dtype for cached left/right column environments (the role of the
+ *   reference's bMPS environment reuse, pureTNS.py:163-2375): a move on a
+ *   horizontal pair then costs two column steps and on a vertical pair one,
+ *   instead of Ly; edges must be nearest-neighbour pairs (else *d_err, device
+ *   int, nullable, = VMC_ERR_UNSUPPORTED).  NULL recomputes every proposal from
+ *   scratch (sign/logabs are then required by the local energy).
  * vmc_peps_logpsi_grad  — O (B, ldo >= Lx*Ly*4*D^4, dtype of prec) =
  *                         d log|psi| / d tensors in the flattened tensor order
  *                         (zero except at each site's occupied state), by a
@@ -259,11 +268,12 @@ int vmc_peps_eval(int prec, const void* tensors, int Lx, int Ly, int D, const ui
 int vmc_peps_sweep(int prec, const void* tensors, int Lx, int Ly, int D, uint64_t* occ, int64_t B,
                    const int32_t* edges, int n_edges, int n_sweeps, float hopping_rate, uint64_t seed,
                    uint64_t sweep_offset, const float* r_move, const uint8_t* r_bit, const float* r_acc, double* sign,
-                   double* logabs, int32_t* n_acc, uint64_t* d_n_eval, void* stream);
+                   double* logabs, int32_t* n_acc, uint64_t* d_n_eval, void* env_work, int64_t work_rows, int* d_err,
+                   void* stream);
 int vmc_peps_local_energy(int prec, const void* tensors, int Lx, int Ly, int D, const uint64_t* occ, int64_t B,
                           const int32_t* edges, double t, double U, const double* sign, const double* logabs,
                           const int32_t* pairs, const int32_t* offs, int64_t P, double* term, double* eloc,
-                          void* stream);
+                          void* env_work, int64_t work_rows, int* d_err, void* stream);
 int vmc_peps_logpsi_grad(int prec, const void* tensors, int Lx, int Ly, int D, const uint64_t* occ, int64_t B,
                          void* O, int64_t ldo, void* work, int64_t work_rows, void* stream);
 

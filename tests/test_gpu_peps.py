@@ -14,9 +14,10 @@ pytestmark = pytest.mark.gpu
 DEV = "cuda"
 
 
-def _model(Lx, Ly, D, T, precision="fp64"):
+def _model(Lx, Ly, D, T, precision="fp64", env=True, env_rows=2048):
     return vg.FPEPS_GB300(Lx, Ly, D, precision=precision, tensors=torch.as_tensor(T),
-                          dtype=torch.float64 if precision == "fp64" else torch.float32).to(DEV)
+                          dtype=torch.float64 if precision == "fp64" else torch.float32, env_reuse=env,
+                          env_rows=env_rows).to(DEV)
 
 
 def _oracle_logamp(T, X):
@@ -59,19 +60,38 @@ def test_peps_zero_amplitude():
     assert torch.all(s == 0) and torch.all(torch.isinf(la)) and torch.all(la < 0)
 
 
-@pytest.mark.parametrize("Lx,Ly,D,nup,B,S", [(4, 2, 4, 2, 64, 3), (6, 4, 2, 6, 32, 2), (6, 6, 4, 16, 6, 1)])
-def test_peps_sweep_vs_oracle_replay(Lx, Ly, D, nup, B, S):
+class _Shuffled:
+    """A graph whose sweep visits the nearest-neighbour edges in a fixed random order."""
+
+    def __init__(self, edges):
+        self.edges = edges
+
+    def device_edges(self, device, kind):
+        return torch.tensor(self.edges, dtype=torch.int32, device=device).reshape(-1, 2)
+
+
+@pytest.mark.parametrize("env", [True, False])
+@pytest.mark.parametrize("Lx,Ly,D,nup,B,S,order", [(4, 2, 4, 2, 64, 3, "sweep"), (6, 4, 2, 6, 32, 2, "sweep"),
+                                                   (6, 6, 4, 16, 6, 1, "sweep"), (6, 4, 2, 6, 24, 2, "shuffled"),
+                                                   (4, 3, 4, 3, 24, 2, "shuffled")])
+def test_peps_sweep_vs_oracle_replay(Lx, Ly, D, nup, B, S, order, env):
     N = Lx * Ly
     rng = np.random.default_rng(N)
     T = peps.init_tensors(Lx, Ly, D, seed=N)
-    g = vg.SquareLattice(Lx, Ly)
-    E = len(g.sweep_edges())
+    edges = lattice.sweep_edges(Lx, Ly)
+    if order == "shuffled":  # arbitrary visiting order (and pair orientation) exercises the cache validity logic
+        perm = rng.permutation(len(edges))
+        edges = [edges[k] if k % 2 else edges[k][::-1] for k in perm]
+        g = _Shuffled(edges)
+    else:
+        g = vg.SquareLattice(Lx, Ly)
+    E = len(edges)
     X = lattice.random_initial_configs(B, N, nup, nup, seed=N + 1)
     um = rng.random((S, E, B), dtype=np.float32)
     hb = rng.integers(0, 2, (S, E, B)).astype(np.uint8)
     ua = rng.random((S, E, B), dtype=np.float32)
-    xo, (so, lo), nacc = osampler.sweep(X, lattice.sweep_edges(Lx, Ly), lambda y: _oracle_logamp(T, y), um, hb, ua)
-    m = _model(Lx, Ly, D, T)
+    xo, (so, lo), nacc = osampler.sweep(X, edges, lambda y: _oracle_logamp(T, y), um, hb, ua)
+    m = _model(Lx, Ly, D, T, env=env, env_rows=max(B // 3, 1))
     smp = vg.MetropolisExchangeSpinfulSamplerGB300()
     fx = torch.as_tensor(X, device=DEV).clone()
     rp = tuple(torch.as_tensor(a, device=DEV).contiguous() for a in (um, hb, ua))
@@ -110,8 +130,9 @@ def test_peps_variational_energy_4x2():
 
 
 def test_peps_fp32_sweep_consistent():
-    """Philox sweeps in FP32 at 6x6, D = 4: the carried log-amplitudes equal a
-    fresh evaluation of the final configurations, and moves are accepted."""
+    """Philox sweeps in FP32 at 6x6, D = 4: the carried log-amplitudes (from the
+    cached environments) agree with a fresh evaluation of the final
+    configurations, and moves are accepted."""
     m = vg.FPEPS_GB300(6, 6, 4, generator=torch.Generator().manual_seed(0)).to(DEV)
     H = vg.spinful_Fermi_Hubbard_square_lattice_torch(6, 6, 1.0, 8.0, 32, n_fermions_per_spin=(16, 16))
     H.precompute_hops_gpu(DEV)
@@ -119,7 +140,8 @@ def test_peps_fp32_sweep_consistent():
     smp = vg.MetropolisExchangeSpinfulSamplerGB300(seed=5)
     fx, (s, la) = smp.step(fx, m, H.graph, use_log_amp=True)
     s2, la2 = m.forward_log(fx)
-    assert torch.equal(s, s2) and torch.equal(la, la2)
+    assert torch.equal(s, s2)
+    torch.testing.assert_close(la, la2, rtol=0, atol=2e-4)  # environment contraction vs a fresh sweep, FP32
     st = m.bind_state(fx)
     assert int(st.n_acc.sum()) > 0
     E, eloc = vg.evaluate_energy(fx, m, H)
@@ -173,3 +195,26 @@ def test_peps_vmc_4x2_energy():
     _, eloc = vg.evaluate_energy(fx, model, H)
     e = eloc.cpu().numpy()
     assert abs(e.mean() - Eex) < 5 * e.std() / np.sqrt(len(e)) + 0.05
+
+
+def test_peps_fp32_env_matches_recompute():
+    """FP32 at 6x6, D = 4 (the register-tiled path): sweeps with environment
+    reuse follow the same chains as full recomputation (acceptance decisions
+    agree except within FP32 rounding of the ratio) and give the same local
+    energies to 1e-4 relative on identical configurations."""
+    T = peps.init_tensors(6, 6, 4, seed=31)
+    H = vg.spinful_Fermi_Hubbard_square_lattice_torch(6, 6, 1.0, 8.0, 32, n_fermions_per_spin=(16, 16))
+    H.precompute_hops_gpu(DEV)
+    x0 = vg.init_walkers(96, 36, 16, 16, seed=6, device=DEV)
+    out = []
+    for env in (True, False):
+        m = _model(6, 6, 4, T.astype(np.float32).astype(np.float64), precision="fp32", env=env, env_rows=40)
+        fx = x0.clone()
+        fx, _ = vg.MetropolisExchangeSpinfulSamplerGB300(seed=9, sweeps_per_step=2).step(fx, m, H.graph)
+        out.append((m, fx))
+    same = (out[0][1] == out[1][1]).all(dim=1)
+    assert same.double().mean().item() >= 0.95
+    x = out[1][1]
+    e_env = vg.evaluate_energy(x.clone(), out[0][0], H)[1]
+    e_full = vg.evaluate_energy(x.clone(), out[1][0], H)[1]
+    torch.testing.assert_close(e_env, e_full, rtol=1e-4, atol=1e-4)

@@ -68,8 +68,9 @@ SIGNATURES = {
     "vmc_gemm": [I32, I32, I64, I64, I64, F64, P, I64, P, I64, P, I32, F64, P, I64, P, I64, I32, P],
     "vmc_sr_kron_correction": [I64, P, I64, P, I64, P, I32, I64, I64, F64, F64, P, P],
     "vmc_peps_eval": [I32, P, I32, I32, I32, P, I64, P, P, P],
-    "vmc_peps_sweep": [I32, P, I32, I32, I32, P, I64, P, I32, I32, F32, U64, U64, P, P, P, P, P, P, P, P],
-    "vmc_peps_local_energy": [I32, P, I32, I32, I32, P, I64, P, F64, F64, P, P, P, P, I64, P, P, P],
+    "vmc_peps_sweep": [I32, P, I32, I32, I32, P, I64, P, I32, I32, F32, U64, U64, P, P, P, P, P, P, P, P, I64, P,
+                       P],
+    "vmc_peps_local_energy": [I32, P, I32, I32, I32, P, I64, P, F64, F64, P, P, P, P, I64, P, P, P, I64, P, P],
     "vmc_peps_logpsi_grad": [I32, P, I32, I32, I32, P, I64, P, I64, P, I64, P],
 }
 

@@ -41,7 +41,8 @@ struct Peps {
   static constexpr int ESZ = DA * D * D * DA;  // environment
   static constexpr int SL = D * D * D * DA;    // per-slice intermediate
   static constexpr int MSZ = DA * D * DA;      // boundary MPS column
-  static constexpr int NW = DA < 16 ? DA : 16; // warps per CTA
+  // warps per CTA (one per top-bond slice; FP64 at DA = 16 takes two slices a warp for registers)
+  static constexpr int NW = (sizeof(T) == 8 && DA > 8) ? 8 : (DA < 16 ? DA : 16);
   static constexpr int NT = 32 * NW;
   static constexpr int R = (SL + 31) / 32;     // outputs per lane per step
   static constexpr bool FAST = std::is_same<T, float>::value && D == 4 && DA == 16;  // register-tiled step
@@ -51,7 +52,12 @@ struct Peps {
   static constexpr size_t off_M = 0, off_N = off_M + MSZ, off_E0 = off_N + MSZ, off_E1 = off_E0 + ESZ,
                           off_buf = off_E1 + ESZ,
                           off_red = off_buf + (size_t)NW * BUFW, off_col = off_red + 32;
-  static size_t smem_bytes(int Lx) { return (off_col + (size_t)Lx * D4) * sizeof(T); }
+  // + 4 broadcast doubles (8-byte aligned) and the environment cache's 2 x 17 exponents
+  static size_t smem_bytes(int Lx) { return (off_col + (size_t)Lx * D4) * sizeof(T) + 8 + 4 * sizeof(double) + 34 * sizeof(int); }
+  static __device__ double* bcast(T* sm, int Lx) {
+    return reinterpret_cast<double*>((reinterpret_cast<uintptr_t>(sm + off_col + (size_t)Lx * D4) + 7) & ~uintptr_t(7));
+  }
+  static __device__ int* exps(T* sm, int Lx) { return reinterpret_cast<int*>(bcast(sm, Lx) + 4); }
 };
 
 __device__ __forceinline__ uint64_t row_mask(int r, int Ly, int c) {  // sites (r, 0..c-1)
@@ -327,71 +333,73 @@ struct SliceStep<float, 4, 16> {
   }
 };
 
-// psi(up, dn) for the CTA.  Every thread returns the same (sign, log|psi|).
+constexpr int EXP_ZERO = INT_MIN, EXP_BAD = INT_MAX;
+
+// One column step of the two-row sweep, CTA-wide: dst = f_c(src) for the
+// configuration (up, dn).  mirror = true contracts from the right (the
+// column's left and right legs exchanged), so right environments F_c =
+// dZ/dE_c come from the same code: F_c = f_c~(F_{c+1}).  src and dst are
+// distinct shared-memory environments.  dst is rescaled by 2^-e in place;
+// returns e, EXP_ZERO when dst vanishes, EXP_BAD when it is not finite.
 template <typename T, int D, int DA>
-__device__ void peps_amp(const T* __restrict__ tens, int Lx, int Ly, uint64_t up, uint64_t dn, T* sm, double& sgn,
-                         double& la) {
+__device__ int col_step(const T* __restrict__ tens, int Lx, int Ly, uint64_t up, uint64_t dn, int c, bool mirror,
+                        const T* src, T* dst, T* sm) {
   using P = Peps<T, D, DA>;
   T* Mc = sm + P::off_M;
   T* Nc = sm + P::off_N;
-  T* E0 = sm + P::off_E0;
-  T* E1 = sm + P::off_E1;
   T* red = sm + P::off_red;
   T* tcol = sm + P::off_col;
+  T* scr = sm + P::off_buf;  // the warps' buffers are free outside the slice step
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   T* buf = sm + P::off_buf + (size_t)warp * P::BUFW;
   const int mid = Lx / 2 - 1;
-  const T* A2 = tcol + (size_t)mid * P::D4;
-  const T* A3 = tcol + (size_t)(mid + 1) * P::D4;
-
-  for (int o = threadIdx.x; o < P::ESZ; o += blockDim.x) E0[o] = (o == 0) ? T(1) : T(0);
-  int expo = 0;
-  T scale = 1;
-  bool zero = false, bad = false;
-  for (int c = 0; c < Ly; ++c) {
-    __syncthreads();  // previous column finished with tcol / M / N / E0
-    // ---- load the column's signed tensors ----
-    for (int o = threadIdx.x; o < Lx * P::D4; o += blockDim.x) {
-      const int r = o / P::D4, idx = o % P::D4;
-      const int site = r * Ly + c;
-      const int s = site_state(up, dn, site);
-      T v = tens[((size_t)site * 4 + s) * P::D4 + idx];
-      if (r > 0) {
-        const int l = idx / (D * D * D), u = (idx / (D * D)) % D;
-        const uint64_t m = row_mask(r, Ly, c);
-        const int nleft = __popcll(up & m) + __popcll(dn & m);
-        if (u & (l ^ nleft) & 1) v = -v;
-      }
-      tcol[o] = v;
+  __syncthreads();  // earlier readers of tcol / M / N / the buffers / src are done
+  for (int o = threadIdx.x; o < Lx * P::D4; o += blockDim.x) {
+    const int r = o / P::D4, idx = o % P::D4;
+    int l = idx / (D * D * D);
+    const int u = (idx / (D * D)) % D, rr = (idx / D) % D, d = idx % D;
+    int sidx = idx;
+    if (mirror) {  // mirrored element (l, u, rr, d) is the original (rr, u, l, d)
+      sidx = ((rr * D + u) * D + l) * D + d;
+      l = rr;
     }
-    __syncthreads();
-    // E1 (the free environment buffer) doubles as the builder's scratch
-    build_boundary<T, D, DA>(tcol, Lx, true, Mc, E1, E1 + P::MSZ, scale, P::FAST);
-    build_boundary<T, D, DA>(tcol, Lx, false, Nc, E1, E1 + P::MSZ, T(1));
-    // ---- per-slice sweep step ----
-    T wmax = 0;
-    for (int b = warp; b < DA; b += P::NW)
-      wmax = fmax(wmax, SliceStep<T, D, DA>::run(Mc, E0, A2, A3, Nc, buf, E1, b, lane));
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) wmax = fmax(wmax, __shfl_xor_sync(VMC_FULL_MASK, wmax, o));
-    if (lane == 0) red[warp] = wmax;
-    __syncthreads();
-    T m = 0;
-    for (int k = 0; k < P::NW; ++k) m = fmax(m, red[k]);
-    T* t = E0; E0 = E1; E1 = t;
-    if (m == T(0)) { zero = true; break; }
-    if (!(m < T(INFINITY))) { bad = true; break; }  // inf / NaN tensors
-    if (c + 1 < Ly) {  // the factor 2^-e enters through the next column's M
-      const int e = exp2_of<T>(m);
-      expo += e;
-      scale = (T)ldexp(1.0, -e);
+    const int site = r * Ly + c;
+    T v = tens[((size_t)site * 4 + site_state(up, dn, site)) * P::D4 + sidx];
+    if (r > 0) {
+      const uint64_t m = row_mask(r, Ly, c);
+      if (u & (l ^ (__popcll(up & m) + __popcll(dn & m))) & 1) v = -v;
     }
+    tcol[o] = v;
   }
   __syncthreads();
+  build_boundary<T, D, DA>(tcol, Lx, true, Mc, scr, scr + P::MSZ, T(1), P::FAST);
+  build_boundary<T, D, DA>(tcol, Lx, false, Nc, scr, scr + P::MSZ, T(1));
+  const T* A2 = tcol + (size_t)mid * P::D4;
+  const T* A3 = tcol + (size_t)(mid + 1) * P::D4;
+  T wmax = 0;
+  for (int b = warp; b < DA; b += P::NW)
+    wmax = fmax(wmax, SliceStep<T, D, DA>::run(Mc, src, A2, A3, Nc, buf, dst, b, lane));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) wmax = fmax(wmax, __shfl_xor_sync(VMC_FULL_MASK, wmax, o));
+  if (lane == 0) red[warp] = wmax;
+  __syncthreads();
+  T m = 0;
+  for (int k = 0; k < P::NW; ++k) m = fmax(m, red[k]);
+  if (m == T(0)) return EXP_ZERO;
+  if (!(m < T(INFINITY))) return EXP_BAD;
+  const int e = exp2_of<T>(m);
+  const T sc = (T)ldexp(1.0, -e);
+  for (int o = threadIdx.x; o < P::ESZ; o += blockDim.x) dst[o] *= sc;
+  return e;
+}
+
+// (sign, log|psi|) from a normalised contraction value v * 2^expo and the
+// configuration's global sign (-1)^{K(K-1)/2}.
+__device__ __forceinline__ void finish_amp(double v, int expo, bool bad, uint64_t up, uint64_t dn, double& sgn,
+                                           double& la) {
   const int K = __popcll(up ^ dn);
   const double g = ((K * (K - 1) / 2) & 1) ? -1.0 : 1.0;
-  const double v = zero ? 0.0 : (double)E0[0];
-  if (bad) {
+  if (bad || !isfinite(v)) {
     sgn = 0.0;
     la = NAN;
   } else if (v == 0.0) {
@@ -401,6 +409,282 @@ __device__ void peps_amp(const T* __restrict__ tens, int Lx, int Ly, uint64_t up
     sgn = v < 0 ? -g : g;
     la = log(fabs(v)) + (double)expo * 0.69314718055994530942;
   }
+}
+
+// finish_amp evaluated once (thread 0) and broadcast: the FP64 log on every
+// thread would occupy GB300's narrow FP64 pipe.
+__device__ __forceinline__ void cta_finish(double v, int expo, bool bad, uint64_t up, uint64_t dn, double& sgn,
+                                           double& la, double* bc) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    finish_amp(v, expo, bad, up, dn, sgn, la);
+    bc[0] = sgn;
+    bc[1] = la;
+  }
+  __syncthreads();
+  sgn = bc[0];
+  la = bc[1];
+}
+
+// Metropolis decision u < |psi'|^2 / |psi|^2, taken by thread 0 and broadcast.
+__device__ __forceinline__ bool cta_accept(float u_acc, double la1, double la, double* bc) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    bool a;
+    if (!(la1 > -INFINITY)) a = false;  // zero or NaN
+    else if (la == -INFINITY) a = true;
+    else a = (double)u_acc < exp(2.0 * (la1 - la));
+    bc[2] = a ? 1.0 : 0.0;
+  }
+  __syncthreads();
+  return bc[2] != 0.0;
+}
+
+// psi(up, dn) for the CTA by a full left-to-right sweep.  Every thread
+// returns the same (sign, log|psi|).
+template <typename T, int D, int DA>
+__device__ void peps_amp(const T* __restrict__ tens, int Lx, int Ly, uint64_t up, uint64_t dn, T* sm, double& sgn,
+                         double& la) {
+  using P = Peps<T, D, DA>;
+  T* E0 = sm + P::off_E0;
+  T* E1 = sm + P::off_E1;
+  __syncthreads();
+  for (int o = threadIdx.x; o < P::ESZ; o += blockDim.x) E0[o] = (o == 0) ? T(1) : T(0);
+  int expo = 0;
+  bool zero = false, bad = false;
+  for (int c = 0; c < Ly; ++c) {
+    const int e = col_step<T, D, DA>(tens, Lx, Ly, up, dn, c, false, E0, E1, sm);
+    T* t = E0; E0 = E1; E1 = t;
+    if (e == EXP_ZERO) { zero = true; break; }
+    if (e == EXP_BAD) { bad = true; break; }
+    expo += e;
+  }
+  __syncthreads();
+  cta_finish(zero ? 0.0 : (double)E0[0], expo, bad, up, dn, sgn, la, P::bcast(sm, Lx));
+}
+
+// ---------------------------------------------------------------------------
+// Environment reuse (the role of the reference's cached boundary
+// environments, vmc_torch/GPU/models/pureTNS.py:163-2375).  Per walker the
+// left environments E_k (columns < k contracted) and right environments F_k
+// (columns >= k) live in a global slab with validity masks; Z = <E_k, F_k>
+// for every cut k.  A horizontal move on columns (c, c+1) costs two column
+// steps from E_c and a dot product with F_{c+2}; a vertical move in column c
+// costs one step from E_c and a dot product with F_{c+1}.  A vertical move
+// that changes the electron parity of row r (and so of row r+1) flips the
+// sign rule of both rows' sites right of column c; by Z2 evenness of the
+// row-r segment right of a cut k that equals the diagonal sign
+// (-1)^{N_r(>=k) + p(h_{r,k})} on F_k, p(h_{r,k}) the parity of the row-r
+// leg of the cut index.  Horizontal moves keep every row count right of
+// column c+1, so F_{c+2} stays valid as is.
+// ---------------------------------------------------------------------------
+template <int D>
+struct Log2 { static constexpr int v = D == 4 ? 2 : 1; };
+
+// parity of the row-r leg inside the cut index o = ((a D + l2) D + l3) DA + a'
+template <int D, int DA>
+__device__ __forceinline__ int cut_leg_parity(int o, int r, int mid) {
+  const int ap = o % DA, l3 = (o / DA) % D, l2 = (o / (DA * D)) % D, a = o / (DA * D * D);
+  if (r < mid) return (a >> (Log2<D>::v * (mid - 1 - r))) & 1;
+  if (r == mid) return l2 & 1;
+  if (r == mid + 1) return l3 & 1;
+  return (ap >> (Log2<D>::v * (r - mid - 2))) & 1;
+}
+
+__device__ __forceinline__ int row_count_from(uint64_t up, uint64_t dn, int r, int Ly, int k) {
+  const uint64_t m = (bits_below(Ly) & ~bits_below(k)) << (r * Ly);  // sites (r, k..Ly-1)
+  return __popcll(up & m) + __popcll(dn & m);
+}
+
+template <typename T, int D, int DA>
+struct EnvCache {
+  using P = Peps<T, D, DA>;
+  T* slab;        // [2 (Ly+1)][ESZ]: E_0..E_Ly, F_0..F_Ly
+  int* pE;        // shared: exponents (E_k = E^_k 2^pE[k])
+  int* pF;
+  uint32_t vE, vF;
+  int Ly;
+  bool bad;
+  unsigned long long ncols;  // column steps executed (uniform across the CTA)
+  __device__ T* Eg(int k) const { return slab + (size_t)k * P::ESZ; }
+  __device__ T* Fg(int k) const { return slab + (size_t)(Ly + 1 + k) * P::ESZ; }
+};
+
+template <typename T>
+__device__ __forceinline__ void cta_copy(T* dst, const T* src, int n) {
+  for (int o = threadIdx.x; o < n; o += blockDim.x) dst[o] = src[o];
+}
+
+template <typename T, int D, int DA>
+__device__ void env_init(EnvCache<T, D, DA>& C) {
+  using P = Peps<T, D, DA>;
+  __syncthreads();
+  for (int o = threadIdx.x; o < P::ESZ; o += blockDim.x) {
+    C.Eg(0)[o] = (o == 0) ? T(1) : T(0);
+    C.Fg(C.Ly)[o] = (o == 0) ? T(1) : T(0);
+  }
+  if (threadIdx.x == 0) { C.pE[0] = 0; C.pF[C.Ly] = 0; }
+  C.vE = 1u;
+  C.vF = 1u << C.Ly;
+  C.bad = false;
+  C.ncols = 0;
+  __syncthreads();
+}
+
+// make E_c valid (S0, S1: shared scratch environments)
+template <typename T, int D, int DA>
+__device__ void env_ensure_E(EnvCache<T, D, DA>& C, const T* tens, int Lx, uint64_t up, uint64_t dn, int c, T* S0,
+                             T* S1, T* sm) {
+  using P = Peps<T, D, DA>;
+  if ((C.vE >> c) & 1u) return;
+  int k = c;
+  while (!((C.vE >> k) & 1u)) --k;  // E_0 is always valid
+  __syncthreads();
+  cta_copy(S0, C.Eg(k), P::ESZ);
+  int pc = C.pE[k];
+  for (int j = k; j < c; ++j) {
+    int e = col_step<T, D, DA>(tens, Lx, C.Ly, up, dn, j, false, S0, S1, sm);
+    ++C.ncols;
+    if (e == EXP_BAD) { C.bad = true; e = 0; }
+    if (e == EXP_ZERO) e = 0;
+    pc += e;
+    __syncthreads();
+    cta_copy(C.Eg(j + 1), S1, P::ESZ);
+    if (threadIdx.x == 0) C.pE[j + 1] = pc;
+    C.vE |= 1u << (j + 1);
+    T* t = S0; S0 = S1; S1 = t;
+  }
+  __syncthreads();
+}
+
+template <typename T, int D, int DA>
+__device__ void env_ensure_F(EnvCache<T, D, DA>& C, const T* tens, int Lx, uint64_t up, uint64_t dn, int c, T* S0,
+                             T* S1, T* sm) {
+  using P = Peps<T, D, DA>;
+  if ((C.vF >> c) & 1u) return;
+  int k = c;
+  while (!((C.vF >> k) & 1u)) ++k;  // F_Ly is always valid
+  __syncthreads();
+  cta_copy(S0, C.Fg(k), P::ESZ);
+  int pc = C.pF[k];
+  for (int j = k - 1; j >= c; --j) {
+    int e = col_step<T, D, DA>(tens, Lx, C.Ly, up, dn, j, true, S0, S1, sm);
+    ++C.ncols;
+    if (e == EXP_BAD) { C.bad = true; e = 0; }
+    if (e == EXP_ZERO) e = 0;
+    pc += e;
+    __syncthreads();
+    cta_copy(C.Fg(j), S1, P::ESZ);
+    if (threadIdx.x == 0) C.pF[j] = pc;
+    C.vF |= 1u << j;
+    T* t = S0; S0 = S1; S1 = t;
+  }
+  __syncthreads();
+}
+
+// sum_o S[o] F[o] (-1)^{nparity + p(row-r leg of o)} (no sign when flip_row < 0),
+// CTA-wide; every thread gets the sum.
+template <typename T, int D, int DA>
+__device__ double env_dot(const T* S, const T* F, int flip_row, int nparity, int mid, T* red, double* bc) {
+  using P = Peps<T, D, DA>;
+  __syncthreads();
+  T acc = 0;
+  for (int o = threadIdx.x; o < P::ESZ; o += blockDim.x) {
+    T v = S[o] * F[o];
+    if (flip_row >= 0 && ((cut_leg_parity<D, DA>(o, flip_row, mid) ^ nparity) & 1)) v = -v;
+    acc += v;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(VMC_FULL_MASK, acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += (double)red[k];
+    bc[3] = t;
+  }
+  __syncthreads();
+  return bc[3];
+}
+
+// Electron-count parity change of row r when site (r, c) goes from state xs to ns.
+__device__ __forceinline__ int row_parity_change(int xs, int ns) { return (__popc(xs) + __popc(ns)) & 1; }
+
+// Proposal on the horizontal pair (r, c)-(r, c+1): x' = (up1, dn1).  Leaves
+// S1 = E'_{c+1} (exponent e1 over E_c) and S0 = E'_{c+2} (e2 over E'_{c+1}).
+template <typename T, int D, int DA>
+__device__ void env_prop_h(EnvCache<T, D, DA>& C, const T* tens, int Lx, uint64_t up, uint64_t dn, uint64_t up1,
+                           uint64_t dn1, int c, T* S0, T* S1, T* sm, int& e1, int& e2, double& sgn, double& la) {
+  env_ensure_F(C, tens, Lx, up, dn, c + 2, S0, S1, sm);
+  env_ensure_E(C, tens, Lx, up, dn, c, S0, S1, sm);
+  cta_copy(S0, C.Eg(c), Peps<T, D, DA>::ESZ);
+  e1 = col_step<T, D, DA>(tens, Lx, C.Ly, up1, dn1, c, false, S0, S1, sm);
+  e2 = (e1 == EXP_ZERO || e1 == EXP_BAD) ? e1 : col_step<T, D, DA>(tens, Lx, C.Ly, up1, dn1, c + 1, false, S1, S0, sm);
+  C.ncols += (e1 == EXP_ZERO || e1 == EXP_BAD) ? 1 : 2;
+  double* bc = Peps<T, D, DA>::bcast(sm, Lx);
+  if (e1 == EXP_BAD || e2 == EXP_BAD || C.bad) { cta_finish(0.0, 0, true, up1, dn1, sgn, la, bc); return; }
+  if (e1 == EXP_ZERO || e2 == EXP_ZERO) { cta_finish(0.0, 0, false, up1, dn1, sgn, la, bc); return; }
+  const double z = env_dot<T, D, DA>(S0, C.Fg(c + 2), -1, 0, Lx / 2 - 1, sm + Peps<T, D, DA>::off_red, bc);
+  cta_finish(z, C.pE[c] + e1 + e2 + C.pF[c + 2], false, up1, dn1, sgn, la, bc);
+}
+
+// Proposal on the vertical pair (r, c)-(r+1, c).  flip: the move changes row
+// r's electron parity.  Leaves S1 = E'_{c+1} (exponent e1 over E_c).
+template <typename T, int D, int DA>
+__device__ void env_prop_v(EnvCache<T, D, DA>& C, const T* tens, int Lx, uint64_t up, uint64_t dn, uint64_t up1,
+                           uint64_t dn1, int r, int c, bool flip, T* S0, T* S1, T* sm, int& e1, double& sgn,
+                           double& la) {
+  env_ensure_F(C, tens, Lx, up, dn, c + 1, S0, S1, sm);
+  env_ensure_E(C, tens, Lx, up, dn, c, S0, S1, sm);
+  cta_copy(S0, C.Eg(c), Peps<T, D, DA>::ESZ);
+  e1 = col_step<T, D, DA>(tens, Lx, C.Ly, up1, dn1, c, false, S0, S1, sm);
+  ++C.ncols;
+  double* bc = Peps<T, D, DA>::bcast(sm, Lx);
+  if (e1 == EXP_BAD || C.bad) { cta_finish(0.0, 0, true, up1, dn1, sgn, la, bc); return; }
+  if (e1 == EXP_ZERO) { cta_finish(0.0, 0, false, up1, dn1, sgn, la, bc); return; }
+  const int np = flip ? (row_count_from(up, dn, r, C.Ly, c + 1) & 1) : 0;
+  const double z =
+      env_dot<T, D, DA>(S1, C.Fg(c + 1), flip ? r : -1, np, Lx / 2 - 1, sm + Peps<T, D, DA>::off_red, bc);
+  cta_finish(z, C.pE[c] + e1 + C.pF[c + 1], false, up1, dn1, sgn, la, bc);
+}
+
+template <typename T, int D, int DA>
+__device__ void env_accept_h(EnvCache<T, D, DA>& C, int c, const T* S0, const T* S1, int e1, int e2) {
+  using P = Peps<T, D, DA>;
+  __syncthreads();
+  cta_copy(C.Eg(c + 1), S1, P::ESZ);
+  cta_copy(C.Eg(c + 2), S0, P::ESZ);
+  if (threadIdx.x == 0) {
+    C.pE[c + 1] = C.pE[c] + e1;
+    C.pE[c + 2] = C.pE[c] + e1 + e2;
+  }
+  C.vE = (C.vE & ((2u << c) - 1u)) | (1u << (c + 1)) | (1u << (c + 2));
+  C.vF &= ~((4u << c) - 1u);  // F_k, k <= c+1, contain the changed columns
+  __syncthreads();
+}
+
+// up1/dn1: the accepted configuration (row counts right of column c equal
+// the old ones).
+template <typename T, int D, int DA>
+__device__ void env_accept_v(EnvCache<T, D, DA>& C, int Lx, int r, int c, bool flip, uint64_t up1, uint64_t dn1,
+                             const T* S1, int e1) {
+  using P = Peps<T, D, DA>;
+  __syncthreads();
+  cta_copy(C.Eg(c + 1), S1, P::ESZ);
+  if (threadIdx.x == 0) C.pE[c + 1] = C.pE[c] + e1;
+  C.vE = (C.vE & ((2u << c) - 1u)) | (1u << (c + 1));
+  C.vF &= ~((2u << c) - 1u);  // F_k, k <= c, contain column c
+  if (flip) {
+    const int mid = Lx / 2 - 1;
+    for (int k = c + 1; k < C.Ly; ++k) {
+      if (!((C.vF >> k) & 1u)) continue;
+      const int np = row_count_from(up1, dn1, r, C.Ly, k) & 1;
+      T* F = C.Fg(k);
+      for (int o = threadIdx.x; o < P::ESZ; o += blockDim.x)
+        if ((cut_leg_parity<D, DA>(o, r, mid) ^ np) & 1) F[o] = -F[o];
+    }
+  }
+  __syncthreads();
 }
 
 // ---- kernels ----
@@ -457,10 +741,7 @@ __global__ void __launch_bounds__(Peps<T, D, DA>::NT)
       double s1, la1;
       peps_amp<T, D, DA>(tens, Lx, Ly, up1, dn1, sm, s1, la1);
       ++ne;
-      bool accept;
-      if (la1 == -INFINITY) accept = false;
-      else if (la == -INFINITY) accept = true;
-      else accept = (double)u_acc < exp(2.0 * (la1 - la));
+      const bool accept = cta_accept(u_acc, la1, la, Peps<T, D, DA>::bcast(sm, Lx));
       if (accept) { up = up1; dn = dn1; sg = s1; la = la1; ++acc; }
     }
   }
@@ -468,7 +749,10 @@ __global__ void __launch_bounds__(Peps<T, D, DA>::NT)
     occ[2 * w] = up; occ[2 * w + 1] = dn;
     sign[w] = sg; logabs[w] = la;
     if (n_acc) n_acc[w] += acc;
-    if (n_eval && ne) atomicAdd(n_eval, ne);
+    if (n_eval && ne) {
+      atomicAdd(n_eval, ne);
+      atomicAdd(n_eval + 1, ne * (unsigned long long)Ly);
+    }
   }
 }
 
@@ -501,6 +785,151 @@ __global__ void __launch_bounds__(Peps<T, D, DA>::NT)
     const double s0 = sign[w], la0 = logabs[w];
     term[p] = (s1 == 0.0) ? 0.0 : coeff * s1 * s0 * exp(la1 - la0);
   }
+}
+
+// Sweeps with environment reuse: one CTA per walker, environments in the
+// walker's slab (chunk-local slot).  Same proposals, random stream and
+// acceptance as k_peps_sweep; edges must be nearest-neighbour pairs (else
+// *d_err = VMC_ERR_UNSUPPORTED and the edge is skipped).
+template <typename T, int D, int DA>
+__global__ void __launch_bounds__(Peps<T, D, DA>::NT)
+    k_peps_sweep_env(const T* __restrict__ tens, int Lx, int Ly, uint64_t* __restrict__ occ, int64_t B, int64_t w0,
+                     const int32_t* __restrict__ edges, int E, int n_sweeps, float hopping_rate, uint64_t seed,
+                     uint64_t sweep_offset, const float* __restrict__ r_move, const uint8_t* __restrict__ r_bit,
+                     const float* __restrict__ r_acc, double* __restrict__ sign, double* __restrict__ logabs,
+                     int32_t* __restrict__ n_acc, unsigned long long* __restrict__ n_eval, T* __restrict__ env,
+                     int* __restrict__ d_err) {
+  using P = Peps<T, D, DA>;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  T* sm = reinterpret_cast<T*>(smraw);
+  const int64_t w = w0 + blockIdx.x;
+  if (w >= B) return;
+  EnvCache<T, D, DA> C;
+  C.slab = env + (size_t)blockIdx.x * (size_t)(2 * (Ly + 1)) * P::ESZ;
+  C.pE = P::exps(sm, Lx);
+  C.pF = C.pE + 17;
+  C.Ly = Ly;
+  T* S0 = sm + P::off_E0;
+  T* S1 = sm + P::off_E1;
+  env_init(C);
+  uint64_t up = occ[2 * w], dn = occ[2 * w + 1];
+  double sg = sign[w], la = logabs[w];
+  int acc = 0;
+  unsigned long long ne = 0;
+  for (int s = 0; s < n_sweeps; ++s) {
+    for (int e = 0; e < E; ++e) {
+      const int i = edges[2 * e], j = edges[2 * e + 1];
+      const int xi = site_state(up, dn, i), xj = site_state(up, dn, j);
+      if (xi == xj) continue;
+      const int lo = i < j ? i : j, hi = i < j ? j : i;
+      const int ri = lo / Ly, ci = lo % Ly, rj = hi / Ly, cj = hi % Ly;
+      const bool horiz = (ri == rj && cj == ci + 1), vert = (ci == cj && rj == ri + 1);
+      if (!horiz && !vert) {
+        if (d_err && threadIdx.x == 0) atomicExch(d_err, (int)VMC_ERR_UNSUPPORTED);
+        continue;
+      }
+      float u_move, u_acc;
+      int bit;
+      if (r_move) {
+        const size_t ridx = ((size_t)s * E + e) * (size_t)B + (size_t)w;
+        u_move = r_move[ridx]; bit = r_bit[ridx] & 1; u_acc = r_acc[ridx];
+      } else {
+        EdgeDraw d = draw_edge(seed, (uint64_t)w, sweep_offset + (uint64_t)s, (uint32_t)e);
+        u_move = d.u_move; bit = d.bit; u_acc = d.u_acc;
+      }
+      int ni, nj;
+      propose_pair(xi, xj, u_move, bit, hopping_rate, ni, nj);
+      const uint64_t mi = 1ull << i, mj = 1ull << j;
+      uint64_t up1 = up & ~(mi | mj), dn1 = dn & ~(mi | mj);
+      if (ni & 2) up1 |= mi;
+      if (ni & 1) dn1 |= mi;
+      if (nj & 2) up1 |= mj;
+      if (nj & 1) dn1 |= mj;
+      double s1, la1;
+      int e1 = 0, e2 = 0;
+      const int xlo = (lo == i) ? xi : xj, nlo = (lo == i) ? ni : nj;
+      const bool flip = vert && row_parity_change(xlo, nlo);
+      if (horiz) env_prop_h(C, tens, Lx, up, dn, up1, dn1, ci, S0, S1, sm, e1, e2, s1, la1);
+      else env_prop_v(C, tens, Lx, up, dn, up1, dn1, ri, ci, flip, S0, S1, sm, e1, s1, la1);
+      ++ne;
+      const bool accept = cta_accept(u_acc, la1, la, P::bcast(sm, Lx));
+      if (accept) {
+        if (horiz) env_accept_h(C, ci, S0, S1, e1, e2);
+        else env_accept_v(C, Lx, ri, ci, flip, up1, dn1, S1, e1);
+        up = up1; dn = dn1; sg = s1; la = la1; ++acc;
+      }
+    }
+  }
+  if (threadIdx.x == 0) {
+    occ[2 * w] = up; occ[2 * w + 1] = dn;
+    sign[w] = sg; logabs[w] = la;
+    if (n_acc) n_acc[w] += acc;
+    if (n_eval) {
+      if (ne) atomicAdd(n_eval, ne);
+      atomicAdd(n_eval + 1, C.ncols);
+    }
+  }
+}
+
+// Local energy with environment reuse: one CTA per walker; all E_k and F_k of
+// x, then every hop term of the walker from them.  psi(x) is taken from the
+// same environments (Z = E_Ly[0]).
+template <typename T, int D, int DA>
+__global__ void __launch_bounds__(Peps<T, D, DA>::NT)
+    k_peps_eloc_env(const T* __restrict__ tens, int Lx, int Ly, const uint64_t* __restrict__ occ, int64_t B,
+                    int64_t w0, const int32_t* __restrict__ pairs, const int32_t* __restrict__ offs,
+                    const int32_t* __restrict__ edges, double t, double U, double* __restrict__ term,
+                    double* __restrict__ eloc, T* __restrict__ env, int* __restrict__ d_err) {
+  using P = Peps<T, D, DA>;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  T* sm = reinterpret_cast<T*>(smraw);
+  const int64_t w = w0 + blockIdx.x;
+  if (w >= B) return;
+  const int N = Lx * Ly;
+  EnvCache<T, D, DA> C;
+  C.slab = env + (size_t)blockIdx.x * (size_t)(2 * (Ly + 1)) * P::ESZ;
+  C.pE = P::exps(sm, Lx);
+  C.pF = C.pE + 17;
+  C.Ly = Ly;
+  T* S0 = sm + P::off_E0;
+  T* S1 = sm + P::off_E1;
+  env_init(C);
+  const uint64_t up = occ[2 * w], dn = occ[2 * w + 1];
+  env_ensure_E(C, tens, Lx, up, dn, Ly, S0, S1, sm);
+  double s0, la0;
+  {
+    __syncthreads();
+    const double z = (double)C.Eg(Ly)[0];
+    cta_finish(z, C.pE[Ly], C.bad, up, dn, s0, la0, P::bcast(sm, Lx));
+  }
+  double tot = U * (double)__popcll(up & dn);
+  for (int q = offs[w]; q < offs[w + 1]; ++q) {
+    const int tm = pairs[2 * q + 1];
+    const int e = tm >> 1, sp = (tm & 1) ? 0 : 1;
+    int i = edges[2 * e], j = edges[2 * e + 1];
+    if (i > j) { const int tt = i; i = j; j = tt; }
+    const int ri = i / Ly, ci = i % Ly, rj = j / Ly, cj = j % Ly;
+    const bool horiz = (ri == rj && cj == ci + 1), vert = (ci == cj && rj == ri + 1);
+    double v = 0.0;
+    if (!horiz && !vert) {
+      if (d_err && threadIdx.x == 0) atomicExch(d_err, (int)VMC_ERR_UNSUPPORTED);
+    } else {
+      const uint64_t m = sp ? up : dn;
+      const int oi = (int)((m >> i) & 1ull);
+      const int base = sp ? 0 : N;
+      uint64_t eu = up, ed = dn;
+      apply_move(eu, ed, N, base + (oi ? i : j), base + (oi ? j : i));
+      const double coeff = symmray_parity(up, dn, i, j, sp) ? t : -t;
+      double s1, la1;
+      int e1 = 0, e2 = 0;
+      if (horiz) env_prop_h(C, tens, Lx, up, dn, eu, ed, ci, S0, S1, sm, e1, e2, s1, la1);
+      else env_prop_v(C, tens, Lx, up, dn, eu, ed, ri, ci, true, S0, S1, sm, e1, s1, la1);  // a hop moves one electron
+      if (threadIdx.x == 0 && s1 != 0.0 && s0 != 0.0) v = coeff * s1 * s0 * exp(la1 - la0);
+    }
+    if (threadIdx.x == 0 && term) term[q] = v;
+    tot += v;
+  }
+  if (threadIdx.x == 0) eloc[w] = tot;
 }
 
 __global__ void k_peps_eloc_reduce(int64_t B, const uint64_t* __restrict__ occ, const int32_t* __restrict__ offs,
@@ -838,7 +1267,7 @@ __global__ void __launch_bounds__(512)
 }
 
 // ---- dispatch over the supported (D, DA) shapes ----
-enum PepsOp { OP_EVAL, OP_SWEEP, OP_TERMS };
+enum PepsOp { OP_EVAL, OP_SWEEP, OP_TERMS, OP_SWEEP_ENV, OP_ELOC_ENV };
 
 struct PepsArgs {
   const void* tens;
@@ -859,6 +1288,13 @@ struct PepsArgs {
   const int32_t* pairs;
   double t;
   double* term;
+  // environment-reuse launches
+  int64_t w0, rows;
+  void* env;
+  int* d_err;
+  const int32_t* offs;
+  double U;
+  double* eloc;
 };
 
 template <typename T, int D, int DA>
@@ -875,10 +1311,20 @@ int launch_peps(PepsOp op, const PepsArgs& a, cudaStream_t st) {
     k_peps_sweep<T, D, DA><<<(unsigned)a.n, P::NT, smem, st>>>(
         tens, a.Lx, a.Ly, a.occ, a.n, a.edges, a.E, a.n_sweeps, a.hopping_rate, a.seed, a.sweep_offset, a.r_move,
         a.r_bit, a.r_acc, a.sign, a.logabs, a.n_acc, a.n_eval);
-  } else {
+  } else if (op == OP_TERMS) {
     cudaFuncSetAttribute(k_peps_conn_terms<T, D, DA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_peps_conn_terms<T, D, DA><<<(unsigned)a.n, P::NT, smem, st>>>(tens, a.Lx, a.Ly, a.occ, a.pairs, a.n,
                                                                      a.edges, a.t, a.sign, a.logabs, a.term);
+  } else if (op == OP_SWEEP_ENV) {
+    cudaFuncSetAttribute(k_peps_sweep_env<T, D, DA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_peps_sweep_env<T, D, DA><<<(unsigned)a.rows, P::NT, smem, st>>>(
+        tens, a.Lx, a.Ly, a.occ, a.n, a.w0, a.edges, a.E, a.n_sweeps, a.hopping_rate, a.seed, a.sweep_offset,
+        a.r_move, a.r_bit, a.r_acc, a.sign, a.logabs, a.n_acc, a.n_eval, (T*)a.env, a.d_err);
+  } else {
+    cudaFuncSetAttribute(k_peps_eloc_env<T, D, DA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_peps_eloc_env<T, D, DA><<<(unsigned)a.rows, P::NT, smem, st>>>(tens, a.Lx, a.Ly, a.occ, a.n, a.w0, a.pairs,
+                                                                      a.offs, a.edges, a.t, a.U, a.term, a.eloc,
+                                                                      (T*)a.env, a.d_err);
   }
   VMC_CUDA_CHECK_LAUNCH();
   return VMC_OK;
@@ -953,10 +1399,11 @@ int vmc_peps_eval(int prec, const void* tensors, int Lx, int Ly, int D, const ui
 int vmc_peps_sweep(int prec, const void* tensors, int Lx, int Ly, int D, uint64_t* occ, int64_t B,
                    const int32_t* edges, int n_edges, int n_sweeps, float hopping_rate, uint64_t seed,
                    uint64_t sweep_offset, const float* r_move, const uint8_t* r_bit, const float* r_acc, double* sign,
-                   double* logabs, int32_t* n_acc, uint64_t* d_n_eval, void* stream) {
+                   double* logabs, int32_t* n_acc, uint64_t* d_n_eval, void* env_work, int64_t work_rows, int* d_err,
+                   void* stream) {
   int rc = check_peps(prec, Lx, Ly, D);
   if (rc) return rc;
-  if (B < 0 || n_edges < 0 || n_sweeps < 0) return VMC_ERR_ARGS;
+  if (B < 0 || n_edges < 0 || n_sweeps < 0 || (env_work && work_rows <= 0)) return VMC_ERR_ARGS;
   if ((r_move != nullptr) != (r_acc != nullptr) || (r_move != nullptr) != (r_bit != nullptr)) return VMC_ERR_ARGS;
   if (B == 0 || n_sweeps == 0 || n_edges == 0) return VMC_OK;
   if (!tensors || !occ || !edges || !sign || !logabs) return VMC_ERR_ARGS;
@@ -965,20 +1412,41 @@ int vmc_peps_sweep(int prec, const void* tensors, int Lx, int Ly, int D, uint64_
   a.n_sweeps = n_sweeps; a.hopping_rate = hopping_rate; a.seed = seed; a.sweep_offset = sweep_offset;
   a.r_move = r_move; a.r_bit = r_bit; a.r_acc = r_acc; a.sign = sign; a.logabs = logabs; a.n_acc = n_acc;
   a.n_eval = (unsigned long long*)d_n_eval;
-  return run_peps(prec, D, OP_SWEEP, a, (cudaStream_t)stream);
+  if (!env_work) return run_peps(prec, D, OP_SWEEP, a, (cudaStream_t)stream);
+  a.env = env_work; a.d_err = d_err;
+  for (int64_t w0 = 0; w0 < B; w0 += work_rows) {
+    a.w0 = w0;
+    a.rows = (B - w0) < work_rows ? (B - w0) : work_rows;
+    rc = run_peps(prec, D, OP_SWEEP_ENV, a, (cudaStream_t)stream);
+    if (rc) return rc;
+  }
+  return VMC_OK;
 }
 
 int vmc_peps_local_energy(int prec, const void* tensors, int Lx, int Ly, int D, const uint64_t* occ, int64_t B,
                           const int32_t* edges, double t, double U, const double* sign, const double* logabs,
                           const int32_t* pairs, const int32_t* offs, int64_t P, double* term, double* eloc,
-                          void* stream) {
+                          void* env_work, int64_t work_rows, int* d_err, void* stream) {
   int rc = check_peps(prec, Lx, Ly, D);
   if (rc) return rc;
-  if (B < 0 || P < 0) return VMC_ERR_ARGS;
+  if (B < 0 || P < 0 || (env_work && work_rows <= 0)) return VMC_ERR_ARGS;
   if (B == 0) return VMC_OK;
-  if (!tensors || !occ || !sign || !logabs || !offs || !eloc || (P > 0 && (!pairs || !edges || !term)))
-    return VMC_ERR_ARGS;
+  if (!tensors || !occ || !offs || !eloc || (P > 0 && (!pairs || !edges))) return VMC_ERR_ARGS;
   cudaStream_t st = (cudaStream_t)stream;
+  if (env_work) {
+    PepsArgs a{};
+    a.tens = tensors; a.Lx = Lx; a.Ly = Ly; a.occ = const_cast<uint64_t*>(occ); a.n = B; a.edges = edges;
+    a.pairs = pairs; a.offs = offs; a.t = t; a.U = U; a.term = term; a.eloc = eloc; a.env = env_work;
+    a.d_err = d_err;
+    for (int64_t w0 = 0; w0 < B; w0 += work_rows) {
+      a.w0 = w0;
+      a.rows = (B - w0) < work_rows ? (B - w0) : work_rows;
+      rc = run_peps(prec, D, OP_ELOC_ENV, a, st);
+      if (rc) return rc;
+    }
+    return VMC_OK;
+  }
+  if (!sign || !logabs || (P > 0 && !term)) return VMC_ERR_ARGS;
   if (P > 0) {
     PepsArgs a{};
     a.tens = tensors; a.Lx = Lx; a.Ly = Ly; a.occ = const_cast<uint64_t*>(occ); a.n = P; a.edges = edges;

@@ -482,10 +482,13 @@ class FPEPS_GB300(WavefunctionModel_GB300):
     precision="fp32": FP32 contraction with power-of-two rescaling per column
     (the production path); "fp64": FP64 (parity mode).
     Init: entries ~ N(0, init_std^2) (config 5 uses N(0, 1)), masked.
+    env_reuse: sweeps and local energies keep each walker's left/right column
+    environments (a workspace of env_rows walkers at a time) and contract only
+    the columns a move touches; False recomputes every amplitude.
     """
 
     def __init__(self, Lx, Ly, D, max_bond=None, dtype=torch.float32, precision="fp32", init_std=1.0,
-                 generator=None, tensors=None):
+                 generator=None, tensors=None, env_reuse=True, env_rows=2048):
         if precision not in _PEPS_PREC:
             raise ValueError("precision must be 'fp32' or 'fp64'")
         if Lx % 2 or not 4 <= Lx <= 8 or D not in (2, 4) or D ** (Lx // 2 - 1) > 16 or Lx * Ly > 64:
@@ -500,6 +503,8 @@ class FPEPS_GB300(WavefunctionModel_GB300):
         self.Lx, self.Ly, self.D = Lx, Ly, D
         self.max_bond = max_bond
         self.precision = precision
+        self.env_reuse = env_reuse
+        self.env_rows = env_rows
         self._cast = None
 
     @staticmethod
@@ -542,7 +547,11 @@ class FPEPS_GB300(WavefunctionModel_GB300):
                   _lib.ptr(st.sign), _lib.ptr(st.logabs), _lib.stream_of(st.device))
 
     def sweep(self, st, graph, n_sweeps, seed, sweep_offset, hopping_rate=0.25, replay=None, n_eval=None):
+        """n_eval: optional int64 CUDA tensor of 2 counters, incremented by the
+        evaluated proposals and by the column steps executed."""
         from .hamiltonian import device_sweep_edges
+        if n_eval is not None and (n_eval.dtype != torch.int64 or n_eval.numel() < 2 or not n_eval.is_cuda):
+            raise ValueError("n_eval must be an int64 CUDA tensor with 2 elements")
         T = self._tensors(st.device)
         edges = device_sweep_edges(graph, st.device)
         rm = rb = ra = None
@@ -552,10 +561,36 @@ class FPEPS_GB300(WavefunctionModel_GB300):
             for a in (rm, rb, ra):
                 if tuple(a.shape) != (n_sweeps, E, st.B) or not a.is_cuda or not a.is_contiguous():
                     raise ValueError("replay buffers must be contiguous CUDA tensors of shape (n_sweeps, E, B)")
+        work, rows, err = self._env_work(st)
         _lib.call("vmc_peps_sweep", self._prec, _lib.ptr(T), *self._shape_args(), _lib.ptr(st.occ), st.B,
                   _lib.ptr(edges), edges.shape[0], int(n_sweeps), float(hopping_rate), int(seed) & ((1 << 64) - 1),
                   int(sweep_offset), _lib.ptr(rm), _lib.ptr(rb), _lib.ptr(ra), _lib.ptr(st.sign), _lib.ptr(st.logabs),
-                  _lib.ptr(st.n_acc), _lib.ptr(n_eval), _lib.stream_of(st.device))
+                  _lib.ptr(st.n_acc), _lib.ptr(n_eval), _lib.ptr(work), rows, _lib.ptr(err),
+                  _lib.stream_of(st.device))
+        self._check_err(err)
+
+    def _env_work(self, st):
+        """(workspace, rows, device error word) for environment reuse, or
+        (None, 0, None) when it is off."""
+        if not self.env_reuse:
+            return None, 0, None
+        rows = int(min(st.B, self.env_rows))
+        da = self.D ** (self.Lx // 2 - 1)
+        n = rows * 2 * (self.Ly + 1) * da * self.D * self.D * da
+        dt = torch.float32 if self._prec == 0 else torch.float64
+        w = st.extra.get("env")
+        if w is None or w.numel() < n or w.dtype != dt:
+            w = torch.empty(n, dtype=dt, device=st.device)
+            st.extra["env"] = w
+            st.extra["env_err"] = torch.zeros(1, dtype=torch.int32, device=st.device)
+        return w, rows, st.extra["env_err"]
+
+    @staticmethod
+    def _check_err(err):
+        if err is not None and int(err.item()) != 0:
+            v = int(err.item())
+            err.zero_()
+            raise ValueError("fPEPS environment reuse needs nearest-neighbour edges (status %d)" % v)
 
     def local_energy(self, st, H):
         T = self._tensors(st.device)
@@ -563,9 +598,12 @@ class FPEPS_GB300(WavefunctionModel_GB300):
         pairs, offs, P = self.conn_pairs(st, H)
         term = torch.empty(max(P, 1), dtype=torch.float64, device=st.device)
         eloc = torch.empty(st.B, dtype=torch.float64, device=st.device)
+        work, rows, err = self._env_work(st)
         _lib.call("vmc_peps_local_energy", self._prec, _lib.ptr(T), *self._shape_args(), _lib.ptr(st.occ), st.B,
                   _lib.ptr(edges), float(H.t), float(H.U), _lib.ptr(st.sign), _lib.ptr(st.logabs), _lib.ptr(pairs),
-                  _lib.ptr(offs), P, _lib.ptr(term), _lib.ptr(eloc), _lib.stream_of(st.device))
+                  _lib.ptr(offs), P, _lib.ptr(term), _lib.ptr(eloc), _lib.ptr(work), rows, _lib.ptr(err),
+                  _lib.stream_of(st.device))
+        self._check_err(err)
         return eloc
 
     def logpsi_grad(self, st, out=None, work_rows=None):
