@@ -25,6 +25,12 @@ Fixtures:
                 evaluate_energy and a column subset + projection of the
                 compute_grads_gpu O matrix.
   minsr.npz     minSR_solver_gpu on a seeded (64 x 96) O and energies.
+  ckpt_nnbf_4x2.pt / ckpt_slater_4x2.pt (+ _stats.json)
+                checkpoints and statistics files written by the reference's
+                run-script callback (make_on_step_end) for 4x2 NNBF_GPU and
+                SlaterDeterminant_GPU models with 6 walkers
+                (``python tests/golden/make_golden.py checkpoints`` rebuilds
+                only these).
 """
 import hashlib
 import os
@@ -257,5 +263,40 @@ def main():
     print("minsr.npz info", info)
 
 
+def make_checkpoints():
+    """ckpt_*.pt: checkpoints written by the reference's own run-script
+    callback (vmc_torch/GPU/run_scripts/vmcconfig.py:185-213) for a 4x2 NNBF_GPU
+    (parameters nnbf_init(8, 8, 256, 2, seed=5)) and a 4x2
+    SlaterDeterminant_GPU (M = N(0,1) from seed 8), each with 6 walkers."""
+    import shutil
+    import tempfile
+    refshim.install()
+    vc = refshim.load("vmc_torch.GPU.run_scripts.vmcconfig")
+    nnbf_mod = refshim.load("vmc_torch.GPU.models.NNBF")
+    slater_mod = refshim.load("vmc_torch.GPU.models.slater")
+    nn_model = nnbf_mod.NNBF_GPU(8, 8, hidden_dim=256, n_layers=2, activation="gelu", bf_scale=0.01)
+    with torch.no_grad():
+        for p, v in zip(nn_model.params, nnbf_init(8, 8, 256, 2, seed=5)):
+            p.copy_(torch.as_tensor(v))
+    sl_model = slater_mod.SlaterDeterminant_GPU(16, 8)
+    with torch.no_grad():
+        sl_model.params[0].copy_(torch.as_tensor(np.random.default_rng(8).standard_normal((16, 8))))
+    fxs = torch.as_tensor(random_initial_configs(6, 8, 4, 4, seed=6))
+    for name, m in (("NNBF", nn_model), ("Slater", sl_model)):
+        with tempfile.TemporaryDirectory() as d:
+            n_params = sum(p.numel() for p in m.parameters())
+            stats = vc.make_stats("4x2 t=1 U=8 N=8", n_params, 6, 1)
+            sf = vc.make_stats_file(d, name, 0)
+            cb = vc.make_on_step_end(0, stats, sf, d, name, m, 1)
+            cb({"step": 0, "energy_per_site": -0.25, "error_per_site": 0.01, "energy_var": 0.5, "fxs": fxs})
+            shutil.copy(os.path.join(d, f"checkpoint_{name}_1.pt"), os.path.join(HERE, f"ckpt_{name.lower()}_4x2.pt"))
+            shutil.copy(sf, os.path.join(HERE, f"ckpt_{name.lower()}_4x2_stats.json"))
+    print("checkpoints written")
+
+
 if __name__ == "__main__":
-    main()
+    if len(sys.argv) > 1 and sys.argv[1] == "checkpoints":
+        make_checkpoints()
+    else:
+        main()
+        make_checkpoints()

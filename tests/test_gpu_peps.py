@@ -185,8 +185,11 @@ def test_peps_vmc_4x2_energy():
     cfg = vg.VMCLoopConfig(vmc_steps=30, ns_per_rank=1024, grad_batch_size=1024, n_params=model.n_params, nsites=8,
                            learning_rate=0.05, diag_shift=1e-3, burn_in_steps=20, outlier_clip_factor=0.0)
     drv = vg.VMC_GB300(smp, vg.MinSRGB300(), vg.SGDGB300(0.05))
-    fx, hist = drv.run_vmc_loop(fx, model, H, H.graph, cfg)
-    assert hist[-1]["energy"] < hist[0]["energy"] - 0.3
+    seen = []
+    hist, fx = drv.run_vmc_loop(fx, model, H, H.graph, 0, 1, cfg, on_step_end=lambda info: seen.append(info))
+    assert [i["step"] for i in seen] == list(range(30)) and seen[-1]["fxs"] is fx
+    assert {"energy_mean", "energy_var", "energy_per_site", "error_per_site", "total_samples"} <= set(seen[0])
+    assert hist[-1] < hist[0] - 0.3 / 8
     S, Hd = hubbard.dense_hamiltonian(8, 4, 4, lattice.square_edges(4, 2), 1.0, 8.0)
     s, la = model.forward_log(torch.as_tensor(S, device=DEV))
     Eex = hubbard.exact_energy((s * torch.exp(la)).cpu().numpy(), Hd)

@@ -167,8 +167,9 @@ def test_vmc_4x2_reaches_exact_energy_of_its_parameters():
     cfg = vg.VMCLoopConfig(vmc_steps=30, ns_per_rank=1024, grad_batch_size=1024, n_params=128, nsites=8,
                            learning_rate=0.1, diag_shift=1e-4, burn_in_steps=50, outlier_clip_factor=0.0)
     drv = vg.VMC_GB300(smp, vg.MinSRGB300(), vg.SGDGB300(0.1))
-    fx, hist = drv.run_vmc_loop(fx, model, H, H.graph, cfg)
-    assert hist[-1]["energy"] < hist[0]["energy"] - 1.0
+    hist, fx = drv.run_vmc_loop(fx, model, H, H.graph, 0, 1, cfg)
+    assert len(hist) == 30 and drv.history[-1]["energy_per_site"] == hist[-1]
+    assert hist[-1] < hist[0] - 1.0 / 8
     S, Hd = hubbard.dense_hamiltonian(8, 4, 4, lattice.square_edges(4, 2), 1.0, 8.0)
     for _ in range(10):
         fx, _ = smp.step(fx, model, H.graph)

@@ -34,6 +34,8 @@ class VMCLoopConfig:
     outlier_clip_factor: float = 100.0
     lr_scheduler: object = None
     verbose: bool = False
+    step_offset: int = 0       # global step of the first iteration (resumed runs)
+    show_progress: bool = False
     factored_o: bool = False   # NNBF: Kronecker-factored out_w block of O (FactoredO)
 
     def __init__(self, **kwargs):
@@ -102,10 +104,23 @@ class VMC_GB300:
         var = (local_energies ** 2).mean() - m * m
         return n, float(m.item()), float(var.item())
 
-    def run_vmc_loop(self, fxs, model, hamiltonian, graph, config: VMCLoopConfig,
+    def run_vmc_loop(self, fxs, model, hamiltonian, graph, rank=0, world_size=1, config: VMCLoopConfig = None,
                      on_step_end: Optional[Callable[[Dict[str, Any]], None]] = None):
+        """The reference's loop contract (vmc_torch/GPU/VMC.py:645-847): returns
+        (energy_history, fxs) with the energy per site of every step, and calls
+        on_step_end with the reference's info keys.  One process drives one GPU
+        (rank 0 of 1); the per-step records with timings are kept in
+        ``self.history``."""
+        if config is None:
+            if isinstance(rank, VMCLoopConfig):  # run_vmc_loop(fxs, model, H, graph, config)
+                config, rank, world_size = rank, 0, 1
+            else:
+                raise ValueError("run_vmc_loop needs a VMCLoopConfig")
+        if world_size != 1:
+            raise ValueError("VMC_GB300 drives one GPU per process (world_size 1)")
         device = next(model.parameters()).device
-        history = []
+        self.history = []
+        energy_history = []
         for step in range(config.vmc_steps):
             t0 = time.time()
             (E, O), fxs, ts, times = self._run_sampling_phase(
@@ -116,12 +131,22 @@ class VMC_GB300:
             dp, t_sr, info = self.preconditioner.solve(
                 local_o=O, local_energies=E, energy_mean=Em, total_samples=n, n_params=config.n_params,
                 diag_shift=config.diag_shift, device=device, run_sr=config.run_sr)
+            global_step = step + config.step_offset
             if config.lr_scheduler is not None:
-                config.learning_rate = config.lr_scheduler(step)
+                config.learning_rate = config.lr_scheduler(global_step)
             self.optimizer.step(model=model, direction=dp, device=device, learning_rate=config.learning_rate)
-            rec = {"step": step, "energy": Em, "energy_per_site": Em / config.nsites, "variance": Evar,
-                   "error": (Evar / n) ** 0.5, "t_step": time.time() - t0, "t_sr": t_sr, "sr_info": info, **times}
-            history.append(rec)
+            t_step = time.time() - t0
+            e_site = Em / config.nsites
+            err = (max(Evar, 0.0) / n) ** 0.5 / config.nsites
+            energy_history.append(e_site)
+            rec = {"step": global_step, "energy": Em, "energy_per_site": e_site, "variance": Evar,
+                   "error": (max(Evar, 0.0) / n) ** 0.5, "t_step": t_step, "t_sr": t_sr, "sr_info": info, **times}
+            self.history.append(rec)
+            if config.show_progress:
+                print("Step %3d | E/site: %.6f +/- %.6f | N=%d | T_samp=%.2fs T_locE=%.2fs T_grad=%.2fs T_SR=%.2fs"
+                      % (global_step, e_site, err, n, times["t_samp"], times["t_locE"], times["t_grad"], t_sr))
             if on_step_end is not None:
-                on_step_end({**rec, "fxs": fxs, "model": model})
-        return fxs, history
+                on_step_end({"step": global_step, "energy_mean": Em, "energy_var": Evar, "energy_per_site": e_site,
+                             "error_per_site": err, "total_samples": n, "sample_time": ts, "phase_times": times,
+                             "sr_time": t_sr, "total_time": t_step, "solver_info": info, "fxs": fxs})
+        return energy_history, fxs
