@@ -192,13 +192,14 @@ def peps_cpu_rate(n_walkers=6, seed=0):
         n_walkers, E)
 
 
-def peps_block(dev, steps, fp32_peak_tflops, cpu=True):
+def peps_block(dev, steps, fp32_peak_tflops, cpu=True, env_reuse=True):
     """Secondary workload: 6x6 OBC Hubbard (16+16), fPEPS D=4 with N(0,1) FP32
     site tensors, 8192 walkers, one Metropolis sweep (60 edges) per step;
     exact contraction (the max_bond -> infinity limit)."""
     import torch
     import vmc_torch_gb300 as vg
-    m = vg.FPEPS_GB300(PEPS_LX, PEPS_LY, PEPS_D, generator=torch.Generator().manual_seed(5)).to(dev)
+    m = vg.FPEPS_GB300(PEPS_LX, PEPS_LY, PEPS_D, generator=torch.Generator().manual_seed(5),
+                       env_reuse=env_reuse).to(dev)
     H = vg.spinful_Fermi_Hubbard_square_lattice_torch(PEPS_LX, PEPS_LY, 1.0, 8.0, 2 * PEPS_NE,
                                                       n_fermions_per_spin=(PEPS_NE, PEPS_NE))
     H.precompute_hops_gpu(dev)
@@ -239,7 +240,7 @@ def peps_block(dev, steps, fp32_peak_tflops, cpu=True):
            "value": steps * PEPS_B * E / (ms / 1e3), "unit": UNIT, "ms_per_step": ms / steps,
            "evaluated_proposals_per_step": n_eval / steps, "column_steps_per_step": n_cols / steps,
            "column_steps_per_proposal": n_cols / max(n_eval, 1),
-           "roofline": {"bound": "fp32 CUDA-core FMA", "kernel": "k_peps_sweep_env<float,4,16>", "achieved": achieved,
+           "roofline": {"bound": "fp32 CUDA-core FMA", "kernel": "k_peps_sweep_env<float,4,16>" if env_reuse else "k_peps_sweep<float,4,16>", "achieved": achieved,
                         "peak": fp32_peak_tflops, "unit": "TFLOP/s", "frac": achieved / fp32_peak_tflops,
                         "algorithmic": "%.4g FLOP per column step (counted on device); a from-scratch amplitude "
                                        "is 6 column steps" % fl,
@@ -486,6 +487,8 @@ def main():
     ap.add_argument("--peps-only", action="store_true",
                     help="run only the fPEPS block (print its JSON object); for profiling")
     ap.add_argument("--peps-walkers", type=int, default=PEPS_B, help="walkers of the fPEPS block (default 8192)")
+    ap.add_argument("--peps-recompute", action="store_true",
+                    help="fPEPS block without cached column environments (every amplitude from scratch)")
     ap.add_argument("--walkers", type=int, default=B,
                     help="walkers per GPU (the headline workload uses 16384; smaller values are for profiling)")
     args = ap.parse_args()
@@ -501,7 +504,7 @@ def main():
         if not os.path.exists(vbuild.LIB):
             vbuild.build()
         print(json.dumps(peps_block(torch.device("cuda", 0), args.steps, 152 * 128 * 2 * 2070e6 / 1e12,
-                                    cpu=False)), flush=True)
+                                    cpu=False, env_reuse=not args.peps_recompute)), flush=True)
         return 0
     return run_gb300(args)
 
