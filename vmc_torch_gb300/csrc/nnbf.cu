@@ -647,6 +647,75 @@ __device__ __forceinline__ void lu_phase(LuRegs<NF>& S, float* prow, int lane) {
   }
 }
 
+// After 32 pivot steps of a 64-row matrix exactly 32 rows are retired.  The
+// live rows move into register slot 0, one per lane in ascending row order
+// (lane L takes the L-th live row), so that the last 32 steps update one row
+// per lane instead of two.  Returns the original row now held by the lane.
+template <int W>
+__device__ __forceinline__ int lu_compact(LuRegs<64>& S, int lane) {
+  uint64_t m = S.U;
+  for (int i = 0; i < lane; ++i) m &= m - 1ull;  // drop the lane's lower live rows
+  const int src = m ? __ffsll((long long)m) - 1 : lane;  // m == 0 only after a failed pivot (result discarded)
+  const int sl = src & 31;
+  const bool s1 = (src >> 5) != 0;
+#pragma unroll
+  for (int c = 0; c < W; ++c) {
+    const float v0 = __shfl_sync(VMC_FULL_MASK, S.a[0][c], sl);
+    const float v1 = __shfl_sync(VMC_FULL_MASK, S.a[1][c], sl);
+    S.a[0][c] = s1 ? v1 : v0;
+  }
+  return src;
+}
+
+// Pivot key over the compacted layout (slot 0 holds original row orow).
+__device__ __forceinline__ unsigned lu_pivot_key_c(const LuRegs<64>& S, int orow) {
+  unsigned key = 0;
+  if ((S.U >> orow) & 1ull) key = (__float_as_uint(fabsf(S.a[0][0])) & ~63u) | (unsigned)(63 - orow);
+  return __reduce_max_sync(VMC_FULL_MASK, key);
+}
+
+// 16 pivot steps over the compacted layout: as lu_phase with one row a lane;
+// the lane holding pivot row p is found by a ballot on the original rows.
+template <int W>
+__device__ __forceinline__ void lu_phase_c(LuRegs<64>& S, float* prow, int lane, int orow) {
+#pragma unroll 1
+  for (int t = 0; t < 16; ++t) {
+    const unsigned key = S.key;
+    const int p = 63 - (int)(key & 63u);
+    const float best = __uint_as_float(key & ~63u);
+    if (orow == p) {
+#pragma unroll
+      for (int q = 0; q < W / 4; ++q)
+        reinterpret_cast<float4*>(prow)[q] =
+            make_float4(S.a[0][4 * q], S.a[0][4 * q + 1], S.a[0][4 * q + 2], S.a[0][4 * q + 3]);
+    }
+    __syncwarp();
+    float pv = prow[0];
+    const bool pvalid = key != 0u && (best > 0.0f) && isfinite(best);
+    if (!pvalid) { S.ok = false; pv = 1.0f; }
+    S.neg ^= (pv < 0.0f);
+    S.neg ^= __popcll(S.U & ((1ull << p) - 1ull)) & 1;
+    S.U &= ~(1ull << p);
+    const float m = S.mant * fabsf(pv);
+    const unsigned mb = __float_as_uint(m);
+    S.expo += (int)((mb >> 23) & 255u) - 127;
+    S.mant = __uint_as_float((mb & 0x007FFFFFu) | 0x3F800000u);
+    const float ipv = __frcp_rn(pv);
+    float pr[W];
+#pragma unroll
+    for (int q = 0; q < W / 4; ++q) {
+      const float4 t4 = reinterpret_cast<const float4*>(prow)[q];
+      pr[4 * q] = t4.x; pr[4 * q + 1] = t4.y; pr[4 * q + 2] = t4.z; pr[4 * q + 3] = t4.w;
+    }
+    const float f = S.a[0][0] * ipv;
+    S.a[0][0] = fmaf(-f, pr[1], S.a[0][1]);
+    S.key = lu_pivot_key_c(S, orow);
+#pragma unroll
+    for (int c = 2; c < W; ++c) S.a[0][c - 1] = fmaf(-f, pr[c], S.a[0][c]);
+    __syncwarp();
+  }
+}
+
 template <int NF>
 __device__ __forceinline__ Det warp_logdet_f32(const float* __restrict__ A, float* prow) {
   static_assert(NF == 32 || NF == 64, "NF must be 32 or 64");
@@ -671,8 +740,9 @@ __device__ __forceinline__ Det warp_logdet_f32(const float* __restrict__ A, floa
   lu_phase<NF, NF>(S, prow, lane);
   lu_phase<NF, NF - 16>(S, prow, lane);
   if constexpr (NF == 64) {
-    lu_phase<NF, 32>(S, prow, lane);
-    lu_phase<NF, 16>(S, prow, lane);
+    const int orow = lu_compact<32>(S, lane);
+    lu_phase_c<32>(S, prow, lane, orow);
+    lu_phase_c<16>(S, prow, lane, orow);
   }
   Det d;
   if (S.ok) {
