@@ -101,6 +101,22 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def replica_rate(units, ms, dist=None, device=None):
+    """Whole-job throughput of independent replicas (one per rank): the units
+    all ranks processed over the slowest rank's time, so that N replicas are
+    timed as one job.  Returns (units/s, max ms).  Collective calls only when
+    a process group is given."""
+    import torch
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    u = torch.tensor([float(units)], dtype=torch.float64, device=device)
+    if dist is not None:
+        dist.barrier()
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    ms_max = float(t.item())
+    return float(u.item()) / (ms_max / 1e3), ms_max
+
+
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -379,13 +395,7 @@ def run_gb300(args):
         torch.cuda.synchronize()
         smp.step(fxs, model, graph, use_log_amp=True, instrument=instr)
     torch.cuda.synchronize()
-    t_max = torch.tensor([total_ms], device=dev)
-    if dist is not None:
-        dist.all_reduce(t_max, op=dist.ReduceOp.MAX)
-        dist.barrier()
-    total_ms = float(t_max.item())
-    wsteps = args.steps * B * E
-    value = wsteps * world / (total_ms / 1e3)
+    value, total_ms = replica_rate(args.steps * B * E, total_ms, dist, dev)
     n_eval = int(instr["n_eval"].item())
     stage_ms = list(instr["stage_ms"])
     stage_n = list(instr["stage_launches"])
@@ -440,7 +450,7 @@ def run_gb300(args):
         e1.record(stream)
         torch.cuda.synchronize()
         e2e_ms += e0.elapsed_time(e1)
-    e2e_value = args.steps * B * E * world / (e2e_ms / 1e3)
+    e2e_value, _ = replica_rate(args.steps * B * E, e2e_ms, dist, dev)
     h2d = B * LX * LY * 8
     d2h = B * LX * LY * 8 + 2 * B * 8
     n_chunks = -(-B // 4096)
