@@ -159,3 +159,33 @@ def test_mixed_chunk_pipeline_is_exact():
     assert bad.double().mean().item() < 0.01
     assert torch.equal(s1[~bad], s2[~bad])
     assert not torch.equal(fx, x)
+
+
+def test_mixed_walker_groups_match_single_stream():
+    """From 8192 walkers the mixed sweep splits the walkers into groups that run
+    their edge loops on separate streams.  Each walker's arithmetic and random
+    draws are unchanged, so a replayed 9000-walker sweep equals, bit for bit,
+    two 4500-walker sweeps (single stream) over the same walkers and draws."""
+    N, nf = 64, 64
+    m = make_model(om.nnbf_init(N, nf, 256, 2, seed=78), N, nf, "mixed")
+    g = vg.SquareLattice(8, 8)
+    E = len(g.sweep_edges())
+    B, S = 9000, 1
+    rng = np.random.default_rng(12)
+    um = torch.as_tensor(rng.random((S, E, B), dtype=np.float32), device=DEV)
+    hb = torch.as_tensor(rng.integers(0, 2, (S, E, B)).astype(np.uint8), device=DEV)
+    ua = torch.as_tensor(rng.random((S, E, B), dtype=np.float32), device=DEV)
+    x = vg.init_walkers(B, N, 32, 32, seed=13, device=DEV)
+    smp = vg.MetropolisExchangeSpinfulSamplerGB300()
+    full = x.clone()
+    full, (s_f, l_f) = smp.step(full, m, g, use_log_amp=True, replay=(um, hb, ua))
+    parts = []
+    for a, b in ((0, 4500), (4500, 9000)):
+        xp = x[a:b].clone()
+        rp = tuple(t[:, :, a:b].contiguous() for t in (um, hb, ua))
+        xp, (sp, lp) = smp.step(xp, m, g, use_log_amp=True, replay=rp)
+        parts.append((xp, sp, lp))
+    assert torch.equal(full, torch.cat([p[0] for p in parts]))
+    assert torch.equal(s_f, torch.cat([p[1] for p in parts]))
+    assert torch.equal(l_f, torch.cat([p[2] for p in parts]))
+    assert not torch.equal(full, x)

@@ -79,15 +79,17 @@ template <> __device__ __forceinline__ float gelu_t<float>(float x) { return gel
 template <> __device__ __forceinline__ double gelu_t<double>(double x) { return gelu_d(x); }
 
 // Sweep prep for edge e of sweep s: proposal, proposed occupation, moves, h1.
+// Walkers [w_begin, w_end) of the B; arrays are indexed by the global walker.
 template <typename T>
-__global__ void k_prep_sweep(int64_t B, int N, const uint64_t* __restrict__ occ, const int32_t* __restrict__ edges,
-                             int e, int s_local, int E, float hop_rate, uint64_t seed, uint64_t sweep_idx,
-                             const float* __restrict__ rm, const uint8_t* __restrict__ rb,
-                             const float* __restrict__ ra, const T* __restrict__ z0, const T* __restrict__ w0t,
-                             uint64_t* __restrict__ prop_occ, PropRec* __restrict__ rec, void* __restrict__ H1) {
+__global__ void k_prep_sweep(int64_t B, int64_t w_begin, int64_t w_end, int N, const uint64_t* __restrict__ occ,
+                             const int32_t* __restrict__ edges, int e, int s_local, int E, float hop_rate,
+                             uint64_t seed, uint64_t sweep_idx, const float* __restrict__ rm,
+                             const uint8_t* __restrict__ rb, const float* __restrict__ ra, const T* __restrict__ z0,
+                             const T* __restrict__ w0t, uint64_t* __restrict__ prop_occ, PropRec* __restrict__ rec,
+                             void* __restrict__ H1) {
   const int lane = threadIdx.x & 31;
-  const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (w >= B) return;
+  const int64_t w = w_begin + (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  if (w >= w_end) return;
   uint64_t up = occ[2 * w], dn = occ[2 * w + 1];
   const int i = edges[2 * e], j = edges[2 * e + 1];
   const int xi = site_state(up, dn, i), xj = site_state(up, dn, j);
@@ -1078,6 +1080,11 @@ struct ChunkPipe {
   cudaStream_t aux = nullptr;
   cudaEvent_t h2 = nullptr, g[2] = {nullptr, nullptr}, lu[2] = {nullptr, nullptr};
   bool ok = false;
+  // walker groups of a sweep (vmc_nnbf_sweep): one stream each, fork/join events
+  static constexpr int kLanes = 4;
+  cudaStream_t lane[kLanes] = {};
+  cudaEvent_t fork = nullptr, join[kLanes] = {};
+  bool lanes_ok = false;
 };
 ChunkPipe g_pipe[16];
 std::mutex g_pipe_mu;
@@ -1102,12 +1109,32 @@ ChunkPipe* chunk_pipe() {
     ok = ok && cudaEventCreateWithFlags(&p.g[i], cudaEventDisableTiming) == cudaSuccess;
     ok = ok && cudaEventCreateWithFlags(&p.lu[i], cudaEventDisableTiming) == cudaSuccess;
   }
+  bool lok = ok && cudaEventCreateWithFlags(&p.fork, cudaEventDisableTiming) == cudaSuccess;
+  for (int i = 0; i < ChunkPipe::kLanes; ++i) {
+    lok = lok && cudaStreamCreateWithFlags(&p.lane[i], cudaStreamNonBlocking) == cudaSuccess;
+    lok = lok && cudaEventCreateWithFlags(&p.join[i], cudaEventDisableTiming) == cudaSuccess;
+  }
+  p.lanes_ok = lok;
   p.ok = ok;
   return ok ? &p : nullptr;
 }
 
+// Walker groups per sweep (VMC_GB300_SWEEP_LANES, 1..4; default 4).  The
+// groups are independent Markov chains, so each runs its whole edge loop on
+// its own stream and the groups' GEMMs, LUs and proposal kernels overlap
+// without a device-wide join per edge.
+int sweep_lanes() {
+  static const int n = [] {
+    const char* e = std::getenv("VMC_GB300_SWEEP_LANES");
+    int v = e ? std::atoi(e) : 4;
+    return v < 1 ? 1 : (v > ChunkPipe::kLanes ? ChunkPipe::kLanes : v);
+  }();
+  return n;
+}
+
 int launch_eval_rows(int prec, int64_t R, int N, int nf, const uint64_t* row_occ, const void* net, double scale,
-                     const Work& wk, int* err, cudaStream_t st, int ldmode, const LdArgs& la) {
+                     const Work& wk, int* err, cudaStream_t st, int ldmode, const LdArgs& la,
+                     bool allow_pipe = true) {
   const int n_orb = 2 * N;
   if (prec == 0) {
     const NetF32& n = *(const NetF32*)net;
@@ -1129,7 +1156,7 @@ int launch_eval_rows(int prec, int64_t R, int N, int nf, const uint64_t* row_occ
     const size_t lsmem = wpb * 64 * sizeof(float);
     // chunk pipeline (two A slots inside the R-row workspace) unless the
     // stages are being timed one by one
-    ChunkPipe* pipe = (n_chunks > 1 && !g_timer.acc) ? chunk_pipe() : nullptr;
+    ChunkPipe* pipe = (allow_pipe && n_chunks > 1 && !g_timer.acc) ? chunk_pipe() : nullptr;
     if (pipe) {
       if (cudaEventRecord(pipe->h2, st) != cudaSuccess || cudaStreamWaitEvent(pipe->aux, pipe->h2, 0) != cudaSuccess)
         return VMC_ERR_CUDA;
@@ -1292,15 +1319,64 @@ int vmc_nnbf_sweep(int prec, const void* const* net_ptrs, int n_sites, int nf, i
   g_timer.acc = stage_ms;
   g_timer.cnt = stage_launches;
   g_timer.used = 0;
+  // walker groups on their own streams (mixed precision, untimed stages, B >= 2 chunks)
+  ChunkPipe* pipe = nullptr;
+  int G = 1;
+  if (prec == 0 && !stage_ms && sweep_lanes() > 1 && B >= 2 * kChunkRows) {
+    pipe = chunk_pipe();
+    if (pipe && pipe->lanes_ok) {
+      G = sweep_lanes();
+      if ((int64_t)G > B / kChunkRows) G = (int)(B / kChunkRows);
+    } else {
+      pipe = nullptr;
+    }
+  }
+  if (G > 1) {
+    if (cudaEventRecord(pipe->fork, st) != cudaSuccess) return VMC_ERR_CUDA;
+    const int64_t Bg = (B + G - 1) / G;
+    const size_t zrow = (size_t)HID * sizeof(float);
+    for (int g = 0; g < G; ++g) {
+      const int64_t w0 = (int64_t)g * Bg, w1 = (w0 + Bg) < B ? (w0 + Bg) : B;
+      if (w0 >= w1) continue;
+      cudaStream_t gs = pipe->lane[g];
+      if (cudaStreamWaitEvent(gs, pipe->fork, 0) != cudaSuccess) return VMC_ERR_CUDA;
+      LdArgs lg = la;
+      lg.rec = la.rec + w0;
+      lg.prop_occ = prop_occ + 2 * w0;
+      lg.occ = occ + 2 * w0;
+      lg.nacc = n_acc + w0;
+      lg.z0 = (char*)z0 + (size_t)w0 * zrow;
+      lg.sign = sign + w0;
+      lg.logabs = logabs + w0;
+      const Work wg{(char*)H1 + (size_t)w0 * HID * 2, (char*)H2 + (size_t)w0 * HID * 2,
+                    (float*)A + (size_t)w0 * nf * nf};
+      const unsigned gwg = (unsigned)(((w1 - w0) * 32 + 255) / 256);
+      for (int s = 0; s < n_sweeps; ++s) {
+        for (int e = 0; e < n_edges; ++e) {
+          k_prep_sweep<float><<<gwg, 256, 0, gs>>>(B, w0, w1, n_sites, occ, edges, e, s, n_edges, hopping_rate, seed,
+                                                   sweep_offset + (uint64_t)s, r_move, r_bit, r_acc,
+                                                   (const float*)z0, nf32.w0t, prop_occ, (PropRec*)rec, H1);
+          int rc = launch_eval_rows(prec, w1 - w0, n_sites, nf, prop_occ + 2 * w0, net, bf_scale, wg, d_err, gs,
+                                    LD_ACCEPT, lg, /*allow_pipe=*/false);
+          if (rc) { g_timer.acc = nullptr; return rc; }
+        }
+      }
+      if (cudaEventRecord(pipe->join[g], gs) != cudaSuccess || cudaStreamWaitEvent(st, pipe->join[g], 0) != cudaSuccess)
+        return VMC_ERR_CUDA;
+    }
+    g_timer.acc = nullptr;
+    VMC_CUDA_CHECK_LAUNCH();
+    return VMC_OK;
+  }
   for (int s = 0; s < n_sweeps; ++s) {
     for (int e = 0; e < n_edges; ++e) {
       STAGE_BEGIN(0);
       if (prec == 0)
-        k_prep_sweep<float><<<gw, 256, 0, st>>>(B, n_sites, occ, edges, e, s, n_edges, hopping_rate, seed,
+        k_prep_sweep<float><<<gw, 256, 0, st>>>(B, 0, B, n_sites, occ, edges, e, s, n_edges, hopping_rate, seed,
                                                 sweep_offset + (uint64_t)s, r_move, r_bit, r_acc, (const float*)z0,
                                                 nf32.w0t, prop_occ, (PropRec*)rec, H1);
       else
-        k_prep_sweep<double><<<gw, 256, 0, st>>>(B, n_sites, occ, edges, e, s, n_edges, hopping_rate, seed,
+        k_prep_sweep<double><<<gw, 256, 0, st>>>(B, 0, B, n_sites, occ, edges, e, s, n_edges, hopping_rate, seed,
                                                  sweep_offset + (uint64_t)s, r_move, r_bit, r_acc,
                                                  (const double*)z0, nf64.w0t, prop_occ, (PropRec*)rec, H1);
       STAGE_END(0);
