@@ -189,3 +189,18 @@ def test_mixed_walker_groups_match_single_stream():
     assert torch.equal(s_f, torch.cat([p[1] for p in parts]))
     assert torch.equal(l_f, torch.cat([p[2] for p in parts]))
     assert not torch.equal(full, x)
+
+
+def test_mixed_local_energy_groups_match_single_stream():
+    """With a workspace of two or more 4096-row chunks the mixed local energy
+    spreads the connected configurations over several streams; the terms are
+    computed exactly as on one stream, so E_loc of 9000 walkers equals that of
+    the two halves evaluated separately, bit for bit."""
+    N, nf = 64, 64
+    m = make_model(om.nnbf_init(N, nf, 256, 2, seed=79), N, nf, "mixed")
+    H = vg.spinful_Fermi_Hubbard_square_lattice_torch(8, 8, 1.0, 8.0, 64, n_fermions_per_spin=(32, 32))
+    H.precompute_hops_gpu(DEV)
+    x = vg.init_walkers(9000, N, 32, 32, seed=14, device=DEV)
+    _, e_full = vg.evaluate_energy(x.clone(), m, H)
+    e_parts = [vg.evaluate_energy(x[a:b].clone(), m, H)[1] for a, b in ((0, 4500), (4500, 9000))]
+    assert torch.equal(e_full, torch.cat(e_parts))

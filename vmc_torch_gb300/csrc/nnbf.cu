@@ -1440,6 +1440,50 @@ int vmc_nnbf_local_energy(int prec, const void* const* net_ptrs, int n_sites, in
                   (const double*)net_ptrs[6]};
     net = &nf64;
   }
+  // Mixed precision with a workspace of >= 2 chunks: the pair chunks are
+  // independent, so G streams each take every G-th sub-chunk with their own
+  // slice of the workspace (the walker-group scheme of vmc_nnbf_sweep).
+  ChunkPipe* pipe = nullptr;
+  int G = 1;
+  if (prec == 0 && !g_timer.acc && sweep_lanes() > 1 && chunk >= 2 * kChunkRows && P > kChunkRows) {
+    pipe = chunk_pipe();
+    if (pipe && pipe->lanes_ok) {
+      G = sweep_lanes();
+      if ((int64_t)G > chunk / kChunkRows) G = (int)(chunk / kChunkRows);
+    }
+  }
+  if (G > 1) {
+    const int64_t sub = chunk / G;
+    if (cudaEventRecord(pipe->fork, st) != cudaSuccess) return VMC_ERR_CUDA;
+    for (int g = 0; g < G; ++g)
+      if (cudaStreamWaitEvent(pipe->lane[g], pipe->fork, 0) != cudaSuccess) return VMC_ERR_CUDA;
+    int64_t k = 0;
+    for (int64_t p0 = 0; p0 < P; p0 += sub, ++k) {
+      const int g = (int)(k % G);
+      cudaStream_t gs = pipe->lane[g];
+      const int64_t R = (P - p0) < sub ? (P - p0) : sub;
+      uint64_t* ro = row_occ + 2 * (size_t)g * sub;
+      double* co = coeff + (size_t)g * sub;
+      const Work wg{(char*)H1 + (size_t)g * sub * HID * 2, (char*)H2 + (size_t)g * sub * HID * 2,
+                    (float*)A + (size_t)g * sub * nf * nf};
+      k_prep_conn<float><<<(unsigned)((R * 32 + 255) / 256), 256, 0, gs>>>(
+          R, n_sites, pairs + 2 * p0, occ, edges, t, (const float*)z0, nf32.w0t, ro, co, wg.H1);
+      LdArgs la{};
+      la.pairs = pairs + 2 * p0;
+      la.coeff = co;
+      la.term = term + p0;
+      la.sign = const_cast<double*>(sign);
+      la.logabs = const_cast<double*>(logabs);
+      int rc = launch_eval_rows(prec, R, n_sites, nf, ro, net, bf_scale, wg, d_err, gs, LD_ELOC, la,
+                                /*allow_pipe=*/false);
+      if (rc) return rc;
+    }
+    for (int g = 0; g < G; ++g)
+      if (cudaEventRecord(pipe->join[g], pipe->lane[g]) != cudaSuccess ||
+          cudaStreamWaitEvent(st, pipe->join[g], 0) != cudaSuccess)
+        return VMC_ERR_CUDA;
+    P = 0;  // every pair is done; only the reduction below remains
+  }
   for (int64_t p0 = 0; p0 < P; p0 += chunk) {
     const int64_t R = (P - p0) < chunk ? (P - p0) : chunk;
     const unsigned gw = (unsigned)((R * 32 + 255) / 256);
