@@ -10,6 +10,7 @@ amplitude data the kernels update in place) bound to the configuration tensor
 it last saw; sampler, local energy and gradients share it.
 """
 import ctypes
+import weakref
 
 import torch
 import torch.nn as nn
@@ -27,15 +28,22 @@ class WalkerState:
         self.sign = torch.empty(B, dtype=torch.float64, device=device)
         self.logabs = torch.empty(B, dtype=torch.float64, device=device)
         self.n_acc = torch.zeros(B, dtype=torch.int32, device=device)
-        self.key = None          # (data_ptr, _version, shape) of the bound config tensor
+        self.key = None          # (weak reference, _version, shape) of the bound config tensor
         self.param_key = None    # model parameter fingerprint at the last refresh
         self.extra = {}
 
     def bound_to(self, fxs):
-        return self.key == (fxs.data_ptr(), fxs._version, tuple(fxs.shape))
+        """True when fxs is the very tensor last bound, unmodified since.  The
+        tensor object is held by a weak reference: a data pointer alone is not
+        enough, because a freed tensor's memory is handed to the next
+        allocation of the same size."""
+        if self.key is None:
+            return False
+        ref, ver, shape = self.key
+        return ref() is fxs and ver == fxs._version and shape == tuple(fxs.shape)
 
     def bind(self, fxs):
-        self.key = (fxs.data_ptr(), fxs._version, tuple(fxs.shape))
+        self.key = (weakref.ref(fxs), fxs._version, tuple(fxs.shape))
 
 
 class WavefunctionModel_GB300(nn.Module):
