@@ -270,13 +270,14 @@ def peps_block(dev, steps, fp32_peak_tflops, cpu=True, env_reuse=True):
 
 
 # ---------------------------------------------------------------------------
-def ess_compare(model, H, fxs, dev, samples=48, moves=28, train_steps=4, epochs=8):
+def ess_compare(model, H, fxs, dev, samples=160, moves=28, train_steps=4, epochs=8, discard=16):
     """ESS/s of E_loc for plain exchange/hop Metropolis (one 112-edge sweep per
     sample) vs the learned proposal (``moves`` MH moves per sample), from the
     same equilibrated walkers at the same parameters.  The proposal is first
     trained on ``train_steps`` x B plain-chain samples.  ESS/s counts sampler
     device time (CUDA events); local energies are evaluated after every sample
-    for the estimator and are not part of either sampler's time."""
+    for the estimator and are not part of either sampler's time.  The first
+    ``discard`` samples of each chain are left out of the estimates."""
     import torch
     import vmc_torch_gb300 as vg
     from vmc_torch_gb300.proposal import LearnedProposal, LearnedSamplerGB300
@@ -311,12 +312,13 @@ def ess_compare(model, H, fxs, dev, samples=48, moves=28, train_steps=4, epochs=
             torch.cuda.synchronize()
             tsum += e0.elapsed_time(e1) / 1e3
             Es.append(vg.evaluate_energy(xc, model, H)[1])
-        E = torch.stack(Es).t().contiguous()
+        E = torch.stack(Es[discard:]).t().contiguous()
         tau = tau_int(E)
-        nb = E.shape[0]
-        return {"ess_per_s": nb * samples / tau / tsum, "tau_int_samples": tau, "sampler_s": tsum,
+        nb, used = E.shape
+        t_used = tsum * used / samples
+        return {"ess_per_s": nb * used / tau / t_used, "tau_int_samples": tau, "sampler_s": tsum,
                 "ms_per_sample": 1e3 * tsum / samples, "energy_per_site": float(E.mean().item()) / (LX * LY),
-                "stderr_per_site": float(E.std().item()) / (LX * LY) * (tau / (nb * samples)) ** 0.5,
+                "stderr_per_site": float(E.std().item()) / (LX * LY) * (tau / (nb * used)) ** 0.5,
                 "split_rhat": split_rhat(E)}
 
     rp = run(plain, x)
@@ -326,7 +328,7 @@ def ess_compare(model, H, fxs, dev, samples=48, moves=28, train_steps=4, epochs=
     return {"plain": rp, "learned": rl, "ess_ratio_learned_over_plain": rl["ess_per_s"] / rp["ess_per_s"],
             "abs_dE_per_site": dE, "matched_energy_1e-3": dE < 1e-3,
             "dE_sigma": dE / (rp["stderr_per_site"] ** 2 + rl["stderr_per_site"] ** 2) ** 0.5,
-            "samples_per_chain": samples, "learned_moves_per_sample": moves, "learned_acceptance": acc,
+            "samples_per_chain": samples, "discarded_per_chain": discard, "learned_moves_per_sample": moves, "learned_acceptance": acc,
             "proposal_train_loss": loss, "proposal_train_s": t_train,
             "proposal": "MLP 128->512->512 GELU (BF16 tcgen05 inference, FP32 CUDA-core training), k<=4 hops"}
 
