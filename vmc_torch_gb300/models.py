@@ -448,21 +448,25 @@ class NNBF_GB300(WavefunctionModel_GB300):
         self.last_conn = {"pairs": pairs, "P": P, "term": term, "t": float(H.t), "occ": st.occ}
         return eloc
 
-    def mh_step(self, st, prop_occ, rec, lg_x=None, lg_p=None, kstats=None):
+    def mh_step(self, st, prop_occ, rec, lg_x=None, lg_p=None, kstats=None, rows=None):
         """Metropolis-Hastings accept of learned proposals (prop_occ, rec from
         ``LearnedProposal.propose``); lg_x rows of moved walkers are replaced by
-        lg_p rows; kstats (8 int32) counts proposals / acceptances by k."""
+        lg_p rows; kstats (8 int32) counts proposals / acceptances by k.
+        rows=(a, b): act on walkers a..b-1 only (prop_occ, rec, lg_x, lg_p are
+        then that group's rows), with their own slice of every buffer, so that
+        disjoint groups may run on different streams."""
         if self.precision != "mixed":
             raise ValueError("the learned-proposal step runs on the mixed-precision model")
         ts, arr = self.net(st.device)
         x = st.extra
         if "z0p" not in x:
             x["z0p"] = torch.empty_like(x["z0"])
+        a, b = rows if rows is not None else (0, st.B)
         _lib.call("vmc_nnbf_mh_step", arr, self.n_sites, self.n_fermions, self.hidden_dim, self.bf_scale,
-                  _lib.ptr(st.occ), st.B, _lib.ptr(prop_occ), _lib.ptr(rec), _lib.ptr(x["z0"]), _lib.ptr(x["z0p"]),
-                  _lib.ptr(st.sign), _lib.ptr(st.logabs), _lib.ptr(st.n_acc), _lib.ptr(x["H1"]), _lib.ptr(x["H2"]),
-                  _lib.ptr(x["A"]), _lib.ptr(lg_x), _lib.ptr(lg_p), _lib.ptr(kstats), _lib.ptr(x["err"]),
-                  _lib.stream_of(st.device))
+                  _lib.ptr(st.occ[a:b]), b - a, _lib.ptr(prop_occ), _lib.ptr(rec), _lib.ptr(x["z0"][a:b]),
+                  _lib.ptr(x["z0p"][a:b]), _lib.ptr(st.sign[a:b]), _lib.ptr(st.logabs[a:b]), _lib.ptr(st.n_acc[a:b]),
+                  _lib.ptr(x["H1"][a:b]), _lib.ptr(x["H2"][a:b]), _lib.ptr(x["A"][a:b]), _lib.ptr(lg_x),
+                  _lib.ptr(lg_p), _lib.ptr(kstats), _lib.ptr(x["err"]), _lib.stream_of(st.device))
 
 
 _PEPS_PREC = {"fp32": 0, "fp64": 1}

@@ -98,13 +98,16 @@ class LearnedProposal:
                         "rec": torch.zeros((R, 12), dtype=torch.int32, device=d)}
         return self._ws
 
-    def logits(self, occ, out=None):
+    def logits(self, occ, out=None, w0=0):
+        """Logits at the R configurations occ; the network's workspace rows
+        [w0, w0 + R) are used (disjoint row ranges may run on different streams)."""
         R = occ.shape[0]
-        w = self._work(R)
+        w = self._work(w0 + R)
         ts, arr = self.inference_weights()
-        L = w["L"][:R] if out is None else out
-        _lib.call("vmc_prop_logits", arr, self.N, _lib.ptr(occ.contiguous()), R, _lib.ptr(w["X"]),
-                  _lib.ptr(w["H1"]), _lib.ptr(w["H2"]), _lib.ptr(L), _lib.ptr(self.err), _lib.stream_of(occ.device))
+        L = w["L"][w0:w0 + R] if out is None else out
+        _lib.call("vmc_prop_logits", arr, self.N, _lib.ptr(occ.contiguous()), R, _lib.ptr(w["X"][w0:w0 + R]),
+                  _lib.ptr(w["H1"][w0:w0 + R]), _lib.ptr(w["H2"][w0:w0 + R]), _lib.ptr(L), _lib.ptr(self.err),
+                  _lib.stream_of(occ.device))
         return L
 
     @property
@@ -115,19 +118,21 @@ class LearnedProposal:
     def k_acc(self):
         return self.kstats[KMAX:].double()
 
-    def propose(self, occ, Lx=None):
+    def propose(self, occ, Lx=None, w0=0):
         """Returns (prop_occ (B, 2), rec (B, 12) int32 records, logits at the
-        proposals) with log q both ways.  Lx: logits at occ if already known."""
+        proposals) with log q both ways.  Lx: logits at occ if already known.
+        w0: first workspace row (walker groups on separate streams use
+        disjoint rows; every call draws from a fresh counter of the stream)."""
         B = occ.shape[0]
-        w = self._work(B)
+        w = self._work(w0 + B)
         s = _lib.stream_of(occ.device)
         if Lx is None:
-            Lx = self.logits(occ, out=w["L"][:B])
-        prop, rec = w["prop"][:B], w["rec"][:B]
+            Lx = self.logits(occ, out=w["L"][w0:w0 + B], w0=w0)
+        prop, rec = w["prop"][w0:w0 + B], w["rec"][w0:w0 + B]
         _lib.call("vmc_prop_sample", _lib.ptr(self.edges), self.E, self.N, _lib.ptr(Lx), _lib.ptr(occ), B,
                   int(self.seed) & ((1 << 64) - 1), self.step_counter, _lib.ptr(prop), _lib.ptr(rec), s)
         self.step_counter += 1
-        Lp = self.logits(prop, out=w["L2"][:B])
+        Lp = self.logits(prop, out=w["L2"][w0:w0 + B], w0=w0)
         _lib.call("vmc_prop_reverse", _lib.ptr(self.edges), self.E, self.N, _lib.ptr(Lp), _lib.ptr(prop), B,
                   _lib.ptr(rec), s)
         return prop, rec, Lp
@@ -196,16 +201,42 @@ class LearnedSamplerGB300(SamplerGB300):
     def __init__(self, proposal, moves_per_step=112):
         self.proposal = proposal
         self.moves_per_step = moves_per_step
+        self._st = []
+
+    def _streams(self, n, device):
+        while len(self._st) < n:
+            self._st.append(torch.cuda.Stream(device=device))
+        return self._st[:n]
+
+    GROUP = 4096   # walkers per group when the batch is split over streams
 
     @torch.inference_mode()
     def step(self, fxs, model, graph=None, use_log_amp=False, **kwargs):
         st = model.bind_state(fxs)
         P = self.proposal
+        B = st.B
+        P._work(B)
         Lx = P.logits(st.occ).clone()   # logits at the current configurations
-        for _ in range(self.moves_per_step):
-            prop, rec, Lp = P.propose(st.occ, Lx)
-            # accepted walkers take x' and its logits (one network evaluation per move)
-            model.mh_step(st, prop, rec, Lx, Lp, P.kstats)
+        if B < 2 * self.GROUP:
+            for _ in range(self.moves_per_step):
+                prop, rec, Lp = P.propose(st.occ, Lx)
+                # accepted walkers take x' and its logits (one network evaluation per move)
+                model.mh_step(st, prop, rec, Lx, Lp, P.kstats)
+        else:
+            # Independent chains: groups of <= 4096 walkers run their moves on
+            # their own streams, so one group's LU overlaps another's GEMMs.
+            groups = [(a, min(B, a + self.GROUP)) for a in range(0, B, self.GROUP)]
+            main = torch.cuda.current_stream(st.device)
+            streams = self._streams(len(groups), st.device)
+            for s in streams:
+                s.wait_stream(main)
+            for _ in range(self.moves_per_step):
+                for (a, b), s in zip(groups, streams):
+                    with torch.cuda.stream(s):
+                        prop, rec, Lp = P.propose(st.occ[a:b], Lx[a:b], w0=a)
+                        model.mh_step(st, prop, rec, Lx[a:b], Lp, P.kstats, rows=(a, b))
+            for s in streams:
+                main.wait_stream(s)
         model.store_configs(st, fxs)
         if use_log_amp:
             return fxs, (st.sign.clone(), st.logabs.clone())
