@@ -456,9 +456,17 @@ def run_gb300(args):
     h2d = B * LX * LY * 8
     d2h = B * LX * LY * 8 + 2 * B * 8
     n_chunks = -(-B // 4096)
-    # per step: the instrumented sweep launches + the per-call refresh (prep, hidden GEMM,
-    # n_chunks x (backflow GEMM + LU)) + the unpack of the configurations
-    gpu_launches = sum(stage_n) + args.steps * (2 + 2 * n_chunks + 1)
+    # Launches of the timed steps.  The sweep runs G walker groups (the library
+    # splits B >= 8192 walkers into min(VMC_GB300_SWEEP_LANES, B // 4096)
+    # groups, default 4), each launching per edge a prep kernel, the hidden
+    # GEMM and (backflow GEMM + LU) per 4096-row chunk of the group; per step
+    # also the refresh (prep, hidden GEMM, n_chunks x (backflow GEMM + LU)) and
+    # the unpack of the configurations.
+    lanes = max(1, min(4, int(os.environ.get("VMC_GB300_SWEEP_LANES", "4"))))
+    G = min(lanes, B // 4096) if B >= 2 * 4096 and lanes > 1 else 1
+    bg = -(-B // G)
+    per_edge = sum(2 + 2 * -(-min(bg, B - g * bg) // 4096) for g in range(G) if g * bg < B)
+    gpu_launches = args.steps * (E * per_edge + 2 + 2 * n_chunks + 1)
 
     ess = ess_compare(model, H, fxs, dev) if not args.no_ess else None
     smax = clocks.get("sm_max_mhz") or 2070.0
