@@ -29,6 +29,11 @@
  *   vmc_peps_eval / _sweep /     — fPEPS_Model_GPU.amplitude / log_amplitude,
  *   _local_energy                  vmc_torch/GPU/models/pureTNS.py:82-146, driven by
  *                                  the same sampler and energy loop as the other models
+ *   vmc_sym_*                    — FermionSymmetryProjectedModel,
+ *                                  vmc_torch/GPU/models/symmetry.py:673-1136
+ *   vmc_propose_edge / _accept_edge, vmc_conn_rows, vmc_eloc_*
+ *                                — the sampler and energy steps for a wrapped model
+ *                                  (vmc_torch/GPU/sampler.py:217-388, vmc_utils.py:322-476)
  */
 #ifndef VMC_GB300_H
 #define VMC_GB300_H
@@ -276,6 +281,46 @@ int vmc_peps_local_energy(int prec, const void* tensors, int Lx, int Ly, int D, 
                           void* env_work, int64_t work_rows, int* d_err, void* stream);
 int vmc_peps_logpsi_grad(int prec, const void* tensors, int Lx, int Ly, int D, const uint64_t* occ, int64_t B,
                          void* O, int64_t ldo, void* work, int64_t work_rows, void* stream);
+
+/* ---- Point-group symmetry projection with fermionic signs
+ * (FermionSymmetryProjectedModel, vmc_torch/GPU/models/symmetry.py:770-1136) ----
+ * psi_r(n) = (1/G) sum_g sign(g, n) chi_r(g) psi(n[perm_g]).
+ * vmc_sym_images:  occ_img (B*G, 2) = the G images of each walker (image site j
+ *   holds site perms[g][j]); fsign (B*G) = sign(g, n) from the inversions of the
+ *   occupied interleaved modes under g^-1 (inv_perms = inverse permutations).
+ * vmc_sym_combine: projected sign/logabs (B) from the images' sign/logabs (B*G)
+ *   and characters (G); weights (B*G, nullable) w_g = sign chi psi_g / (G psi_r),
+ *   so that O_r = sum_g w_g O_g.
+ * vmc_sym_grad_combine: O (B, ldo) = sum_g w_g O_img[b*G+g]; dtype 0 f64, 1 f32. */
+int vmc_sym_images(const uint64_t* occ, int64_t B, int n_sites, const int32_t* perms, const int32_t* inv_perms, int G,
+                   uint64_t* occ_img, double* fsign, void* stream);
+int vmc_sym_combine(const double* sign_img, const double* logabs_img, const double* fsign, const double* chars,
+                    int64_t B, int G, double* sign, double* logabs, double* weights, void* stream);
+int vmc_sym_grad_combine(int dtype, const void* O_img, int64_t ld_img, const double* weights, int64_t B, int G,
+                         int64_t Np, void* O, int64_t ldo, void* stream);
+/* Model-agnostic sweep and local-energy steps (any model that evaluates
+ * batches), used for wrapped models such as the projection:
+ * vmc_propose_edge: the proposal of the sweeps on edge e (same draws; replay or
+ *   Philox), prop_occ (B, 2), u_acc (B), flag (B) = proposal changes the walker.
+ * vmc_accept_edge: Metropolis accept of flagged walkers from the proposals'
+ *   sign/logabs (MetropolisExchangeSpinfulSamplerGPU.step,
+ *   vmc_torch/GPU/sampler.py:342-367).
+ * vmc_conn_rows / vmc_eloc_terms / vmc_eloc_reduce: connected configuration and
+ *   H element per (walker, hop) pair, the terms H psi(x')/psi(x), and
+ *   E_loc = U * doublons + sum of the walker's terms
+ *   (_evaluate_energy_impl, vmc_torch/GPU/vmc_utils.py:322-476). */
+int vmc_propose_edge(const uint64_t* occ, int64_t B, int n_sites, const int32_t* edges, int n_edges, int e, int s,
+                     float hopping_rate, uint64_t seed, uint64_t sweep_index, const float* r_move, const uint8_t* r_bit,
+                     const float* r_acc, uint64_t* prop_occ, float* u_acc, uint8_t* flag, void* stream);
+int vmc_accept_edge(uint64_t* occ, int64_t B, const uint64_t* prop_occ, const float* u_acc, const uint8_t* flag,
+                    const double* sign_p, const double* logabs_p, double* sign, double* logabs, int32_t* n_acc,
+                    void* stream);
+int vmc_conn_rows(const int32_t* pairs, int64_t P, const uint64_t* occ, int n_sites, const int32_t* edges, double t,
+                  uint64_t* row_occ, double* coeff, void* stream);
+int vmc_eloc_terms(const int32_t* pairs, int64_t P, const double* coeff, const double* sign_p, const double* logabs_p,
+                   const double* sign, const double* logabs, double* term, void* stream);
+int vmc_eloc_reduce(const uint64_t* occ, int64_t B, const int32_t* offs, const double* term, double U, double* eloc,
+                    void* stream);
 
 #ifdef __cplusplus
 }

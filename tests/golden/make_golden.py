@@ -31,6 +31,10 @@ Fixtures:
                 SlaterDeterminant_GPU models with 6 walkers
                 (``python tests/golden/make_golden.py checkpoints`` rebuilds
                 only these).
+  sym.npz       FermionSymmetryProjectedModel over SlaterDeterminant_GPU on 4x2
+                (C2v) and 4x4 (C4v): permutations, fermionic signs and
+                forward_log for the four 1D irreps (``... symmetry`` rebuilds
+                only this one).
 """
 import hashlib
 import os
@@ -263,6 +267,47 @@ def main():
     print("minsr.npz info", info)
 
 
+def make_symmetry():
+    """sym.npz: FermionSymmetryProjectedModel (vmc_torch/GPU/models/symmetry.py)
+    over a SlaterDeterminant_GPU base (M ~ N(0,1), seed 3) on 4x2 (C2v) and 4x4
+    (C4v): site permutations, compute_fermion_signs and forward_log for every
+    irrep on 24 configurations (argsort made stable, as for nnbf.npz)."""
+    refshim.install()
+    sym = refshim.load("vmc_torch.GPU.models.symmetry")
+    slater_mod = refshim.load("vmc_torch.GPU.models.slater")
+    orig_argsort = torch.Tensor.argsort
+
+    def stable_argsort(self, dim=-1, descending=False, stable=False):
+        return orig_argsort(self, dim=dim, descending=descending, stable=True)
+
+    torch.Tensor.argsort = stable_argsort
+    out = {}
+    for (Lx, Ly, nup) in ((4, 2, 4), (4, 4, 8)):
+        N = Lx * Ly
+        tag = "%dx%d" % (Lx, Ly)
+        M = np.random.default_rng(3).standard_normal((2 * N, 2 * nup))
+        m = slater_mod.SlaterDeterminant_GPU(2 * N, 2 * nup)
+        with torch.no_grad():
+            m.params[0].copy_(torch.as_tensor(M))
+        X = random_initial_configs(24, N, nup, nup, seed=2)
+        perms, chars, _ = sym.build_symmetry_group(Lx, Ly)
+        out[tag + "_M"] = M
+        out[tag + "_x"] = X.astype(np.int8)
+        out[tag + "_perms"] = perms.numpy()
+        for irrep in ("A1", "A2", "B1", "B2"):
+            pm = sym.FermionSymmetryProjectedModel(m, Lx, Ly, irrep=irrep)
+            with torch.no_grad():
+                sg, la = pm.forward_log(torch.as_tensor(X))
+            out[tag + "_" + irrep + "_chars"] = np.asarray(chars[irrep], dtype=np.float64)
+            out[tag + "_" + irrep + "_sign"] = sg.numpy()
+            out[tag + "_" + irrep + "_logabs"] = la.numpy()
+            if irrep == "A1":
+                out[tag + "_fsign"] = sym.compute_fermion_signs(torch.as_tensor(X), pm.mode_inv_masks).numpy()
+    torch.Tensor.argsort = orig_argsort
+    np.savez_compressed(os.path.join(HERE, "sym.npz"), **out)
+    print("sym.npz written")
+
+
 def make_checkpoints():
     """ckpt_*.pt: checkpoints written by the reference's own run-script
     callback (vmc_torch/GPU/run_scripts/vmcconfig.py:185-213) for a 4x2 NNBF_GPU
@@ -297,6 +342,9 @@ def make_checkpoints():
 if __name__ == "__main__":
     if len(sys.argv) > 1 and sys.argv[1] == "checkpoints":
         make_checkpoints()
+    elif len(sys.argv) > 1 and sys.argv[1] == "symmetry":
+        make_symmetry()
     else:
         main()
         make_checkpoints()
+        make_symmetry()

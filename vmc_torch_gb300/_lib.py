@@ -72,6 +72,14 @@ SIGNATURES = {
                        P],
     "vmc_peps_local_energy": [I32, P, I32, I32, I32, P, I64, P, F64, F64, P, P, P, P, I64, P, P, P, I64, P, P],
     "vmc_peps_logpsi_grad": [I32, P, I32, I32, I32, P, I64, P, I64, P, I64, P],
+    "vmc_sym_images": [P, I64, I32, P, P, I32, P, P, P],
+    "vmc_sym_combine": [P, P, P, P, I64, I32, P, P, P, P],
+    "vmc_sym_grad_combine": [I32, P, I64, P, I64, I32, I64, P, I64, P],
+    "vmc_propose_edge": [P, I64, I32, P, I32, I32, I32, F32, U64, U64, P, P, P, P, P, P, P],
+    "vmc_accept_edge": [P, I64, P, P, P, P, P, P, P, P, P],
+    "vmc_conn_rows": [P, I64, P, I32, P, F64, P, P, P],
+    "vmc_eloc_terms": [P, I64, P, P, P, P, P, P, P],
+    "vmc_eloc_reduce": [P, I64, P, P, F64, P, P],
 }
 
 _lib = None
