@@ -556,14 +556,21 @@ struct Det { double logabs; double sign; };
 //
 // Code-size-aware schedule: the elimination runs in NF/16 phases of 16 steps.
 // Within a phase of width W the live columns of every row are kept at
-// register indices 0..W-1 and rotate by one per step (the shift is fused into
-// the update FMA: a[c-1] = a[c] - f * pivot[c]), so the step body has only
-// compile-time register indices and runs as a runtime loop; each phase is a
-// separate instantiation with W = NF, NF-16, ... (work per step ~ 2 W FMAs
-// instead of the fixed 2 NF).
+// register indices 0..W-1, so the step bodies have only compile-time register
+// indices and run in a runtime loop; each phase is a separate instantiation
+// with W = NF, NF-16, ... (work per step ~ 2 W FMAs instead of the fixed
+// 2 NF).  Columns are held in pairs.  The loop body is two pivot steps: the
+// first eliminates column 0 and updates the pairs in place with the packed
+// FP32 FMA (two correctly rounded FMAs per instruction: results equal the
+// scalar form bit for bit); the second eliminates column 1 and writes every
+// pair one slot lower (pair[i-1] = pair[i] - f * pivot[i]) with scalar FMAs,
+// so the live window stays at the front without register moves.  Packing the
+// shifting step too, or unrolling four steps, raises the register count past
+// 168 (3 CTAs of 4 warps per SM) or the loop body's code size, and measured
+// slower end to end.
 template <int NF>
 struct LuRegs {
-  float a[NF / 32][NF];
+  float2 a[NF / 32][NF / 2];
   uint64_t U;
   float mant;
   int expo, neg;
@@ -571,81 +578,145 @@ struct LuRegs {
   unsigned key;  // pivot key of the next step (computed one step ahead)
 };
 
+// Resident 4-warp CTAs per SM that the LU kernel's register budget is held
+// to (168 registers, no spills).
+constexpr int LU_MIN_CTAS = 3;
+template <int E> __device__ __forceinline__ float lu_el(const float2& v) { return E ? v.y : v.x; }
+
 // Pivot key: max |a| over unretired rows by a single warp reduction on a packed
 // key (|a| bits with the low 6 mantissa bits replaced by 63 - row: larger
 // magnitude wins, ties -> smaller row).  The 6 dropped bits only matter for
 // magnitudes equal to 2^-17 relative, where either choice is a valid pivot.
-template <int NF>
-__device__ __forceinline__ unsigned lu_pivot_key(const LuRegs<NF>& S, int lane) {
+// The pivot column is element E of pair P.  COMPACT: one row a lane, slot 0
+// holding original row orow.
+template <int NF, int R, int P, int E, bool COMPACT>
+__device__ __forceinline__ unsigned lu_pivot_key(const LuRegs<NF>& S, int lane, int orow) {
   unsigned key = 0;
 #pragma unroll
-  for (int r = 0; r < NF / 32; ++r) {
-    const int row = lane + 32 * r;
+  for (int r = 0; r < R; ++r) {
+    const int row = COMPACT ? orow : lane + 32 * r;
     if ((S.U >> row) & 1ull) {
-      const unsigned kb = (__float_as_uint(fabsf(S.a[r][0])) & ~63u) | (unsigned)(63 - row);
+      const unsigned kb = (__float_as_uint(fabsf(lu_el<E>(S.a[r][P]))) & ~63u) | (unsigned)(63 - row);
       key = kb > key ? kb : key;
     }
   }
   return __reduce_max_sync(VMC_FULL_MASK, key);
 }
 
-template <int NF, int W>
-__device__ __forceinline__ void lu_phase(LuRegs<NF>& S, float* prow, int lane) {
-  constexpr int R = NF / 32;
+// Bookkeeping of one pivot step on the pivot value pv read back from the
+// pivot row: validity, sign, retired mask, |det| as mantissa in [1, 2) times
+// 2^expo (normal floats; pivots are O(1e-3..1e1) here, far from the FP32
+// limits).  Returns 1 / pv.
+template <int NF>
+__device__ __forceinline__ float lu_pivot_update(LuRegs<NF>& S, unsigned key, int p, float pv) {
+  const float best = __uint_as_float(key & ~63u);
+  const bool pvalid = key != 0u && (best > 0.0f) && isfinite(best);
+  if (!pvalid) { S.ok = false; pv = 1.0f; }
+  S.neg ^= (pv < 0.0f);
+  S.neg ^= __popcll(S.U & ((1ull << p) - 1ull)) & 1;
+  S.U &= ~(1ull << p);
+  const float m = S.mant * fabsf(pv);
+  const unsigned mb = __float_as_uint(m);
+  S.expo += (int)((mb >> 23) & 255u) - 127;
+  S.mant = __uint_as_float((mb & 0x007FFFFFu) | 0x3F800000u);
+  return __frcp_rn(pv);
+}
+
+// Pivot row (H pairs of the owning lane's register row) -> shared memory.
+template <int H>
+__device__ __forceinline__ void lu_store_row(const float2* a, float* prow) {
+#pragma unroll
+  for (int q = 0; q < H / 2; ++q)
+    reinterpret_cast<float4*>(prow)[q] = make_float4(a[2 * q].x, a[2 * q].y, a[2 * q + 1].x, a[2 * q + 1].y);
+}
+
+// pair[i] -= f * pivot[i] in place for pairs I0 <= i < H, packed FMAs, the
+// pivot row streamed from shared memory (16-byte loads where aligned).
+// pair[i] -= f * pivot[i] in place for pairs 1 <= i < H, packed FMAs, the
+// pivot row streamed from shared memory (16-byte loads where aligned).
+template <int R, int H, int NP>
+__device__ __forceinline__ void lu_update_inplace(float2 (*a)[NP], const float* prow, const float (&f)[R]) {
+  {
+    const float2 p0 = reinterpret_cast<const float2*>(prow)[1];
+#pragma unroll
+    for (int r = 0; r < R; ++r) a[r][1] = __ffma2_rn(make_float2(-f[r], -f[r]), p0, a[r][1]);
+  }
+#pragma unroll
+  for (int q = 1; q < H / 2; ++q) {
+    const float4 t4 = reinterpret_cast<const float4*>(prow)[q];
+    const float2 p0 = make_float2(t4.x, t4.y), p1 = make_float2(t4.z, t4.w);
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const float2 nf2 = make_float2(-f[r], -f[r]);
+      a[r][2 * q] = __ffma2_rn(nf2, p0, a[r][2 * q]);
+      a[r][2 * q + 1] = __ffma2_rn(nf2, p1, a[r][2 * q + 1]);
+    }
+  }
+}
+
+// pair[i-1] = pair[i] - f * pivot[i] for pairs 2 <= i < H, scalar FMAs (the
+// caller has done pair 1 first: it carries the next pivot column).
+template <int R, int H, int NP>
+__device__ __forceinline__ void lu_update_shift(float2 (*a)[NP], const float* prow, const float (&f)[R]) {
+#pragma unroll
+  for (int q = 1; q < H / 2; ++q) {
+    const float4 t4 = reinterpret_cast<const float4*>(prow)[q];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      a[r][2 * q - 1].x = fmaf(-f[r], t4.x, a[r][2 * q].x);
+      a[r][2 * q - 1].y = fmaf(-f[r], t4.y, a[r][2 * q].y);
+      a[r][2 * q].x = fmaf(-f[r], t4.z, a[r][2 * q + 1].x);
+      a[r][2 * q].y = fmaf(-f[r], t4.w, a[r][2 * q + 1].y);
+    }
+  }
+}
+
+// One pivot step on column K (0 or 1) of a phase of width W.  The next pivot
+// column is updated first so that its key reduction overlaps the rest.
+template <int NF, int R, int W, int K, bool COMPACT>
+__device__ __forceinline__ void lu_step(LuRegs<NF>& S, float* prow, int lane, int orow) {
+  constexpr int H = W / 2;
+  const unsigned key = S.key;
+  const int p = 63 - (int)(key & 63u);
+  // pivot row -> shared memory (warp-uniform branch on the register row)
+  if (COMPACT) {
+    if (orow == p) lu_store_row<H>(S.a[0], prow);
+  } else if (R > 1 && (p >> 5)) {
+    if ((p & 31) == lane) lu_store_row<H>(S.a[R - 1], prow);
+  } else {
+    if ((p & 31) == lane) lu_store_row<H>(S.a[0], prow);
+  }
+  __syncwarp();
+  const float ipv = lu_pivot_update<NF>(S, key, p, prow[K]);
+  float f[R];
+#pragma unroll
+  for (int r = 0; r < R; ++r) f[r] = lu_el<K>(S.a[r][0]) * ipv;   // retired rows keep updating harmlessly
+  if constexpr (K == 0) {
+    const float pn = prow[1];
+#pragma unroll
+    for (int r = 0; r < R; ++r) S.a[r][0].y = fmaf(-f[r], pn, S.a[r][0].y);
+    S.key = lu_pivot_key<NF, R, 0, 1, COMPACT>(S, lane, orow);
+    lu_update_inplace<R, H>(S.a, prow, f);
+  } else {
+    const float2 pn = reinterpret_cast<const float2*>(prow)[1];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      S.a[r][0].x = fmaf(-f[r], pn.x, S.a[r][1].x);
+      S.a[r][0].y = fmaf(-f[r], pn.y, S.a[r][1].y);
+    }
+    S.key = lu_pivot_key<NF, R, 0, 0, COMPACT>(S, lane, orow);
+    lu_update_shift<R, H>(S.a, prow, f);
+  }
+  __syncwarp();
+}
+
+// 16 pivot steps of width W (COMPACT: one row a lane, see lu_compact).
+template <int NF, int R, int W, bool COMPACT>
+__device__ __forceinline__ void lu_phase(LuRegs<NF>& S, float* prow, int lane, int orow) {
 #pragma unroll 1
-  for (int t = 0; t < 16; ++t) {
-    const unsigned key = S.key;
-    const int p = 63 - (int)(key & 63u);
-    const float best = __uint_as_float(key & ~63u);
-    // pivot row -> shared memory (warp-uniform branch on the register row)
-    if (R > 1 && (p >> 5)) {
-      if ((p & 31) == lane) {
-#pragma unroll
-        for (int q = 0; q < W / 4; ++q)
-          reinterpret_cast<float4*>(prow)[q] =
-              make_float4(S.a[R - 1][4 * q], S.a[R - 1][4 * q + 1], S.a[R - 1][4 * q + 2], S.a[R - 1][4 * q + 3]);
-      }
-    } else {
-      if ((p & 31) == lane) {
-#pragma unroll
-        for (int q = 0; q < W / 4; ++q)
-          reinterpret_cast<float4*>(prow)[q] =
-              make_float4(S.a[0][4 * q], S.a[0][4 * q + 1], S.a[0][4 * q + 2], S.a[0][4 * q + 3]);
-      }
-    }
-    __syncwarp();
-    float pv = prow[0];
-    const bool pvalid = key != 0u && (best > 0.0f) && isfinite(best);
-    if (!pvalid) { S.ok = false; pv = 1.0f; }
-    S.neg ^= (pv < 0.0f);
-    S.neg ^= __popcll(S.U & ((1ull << p) - 1ull)) & 1;
-    S.U &= ~(1ull << p);
-    // |det| as mantissa in [1, 2) times 2^expo (normal floats; pivots are
-    // O(1e-3..1e1) here, far from the FP32 limits)
-    const float m = S.mant * fabsf(pv);
-    const unsigned mb = __float_as_uint(m);
-    S.expo += (int)((mb >> 23) & 255u) - 127;
-    S.mant = __uint_as_float((mb & 0x007FFFFFu) | 0x3F800000u);
-    const float ipv = __frcp_rn(pv);
-    float pr[W];
-#pragma unroll
-    for (int q = 0; q < W / 4; ++q) {
-      const float4 t4 = reinterpret_cast<const float4*>(prow)[q];
-      pr[4 * q] = t4.x; pr[4 * q + 1] = t4.y; pr[4 * q + 2] = t4.z; pr[4 * q + 3] = t4.w;
-    }
-    float f[R];
-#pragma unroll
-    for (int r = 0; r < R; ++r) {
-      f[r] = S.a[r][0] * ipv;   // retired rows keep updating harmlessly
-      S.a[r][0] = fmaf(-f[r], pr[1], S.a[r][1]);   // next pivot column first ...
-    }
-    S.key = lu_pivot_key<NF>(S, lane);             // ... so its reduction overlaps the rest
-#pragma unroll
-    for (int r = 0; r < R; ++r) {
-#pragma unroll
-      for (int c = 2; c < W; ++c) S.a[r][c - 1] = fmaf(-f[r], pr[c], S.a[r][c]);
-    }
-    __syncwarp();
+  for (int t = 0; t < 8; ++t) {
+    lu_step<NF, R, W, 0, COMPACT>(S, prow, lane, orow);
+    lu_step<NF, R, W, 1, COMPACT>(S, prow, lane, orow);
   }
 }
 
@@ -661,61 +732,14 @@ __device__ __forceinline__ int lu_compact(LuRegs<64>& S, int lane) {
   const int sl = src & 31;
   const bool s1 = (src >> 5) != 0;
 #pragma unroll
-  for (int c = 0; c < W; ++c) {
-    const float v0 = __shfl_sync(VMC_FULL_MASK, S.a[0][c], sl);
-    const float v1 = __shfl_sync(VMC_FULL_MASK, S.a[1][c], sl);
-    S.a[0][c] = s1 ? v1 : v0;
+  for (int i = 0; i < W / 2; ++i) {
+    const float x0 = __shfl_sync(VMC_FULL_MASK, S.a[0][i].x, sl);
+    const float y0 = __shfl_sync(VMC_FULL_MASK, S.a[0][i].y, sl);
+    const float x1 = __shfl_sync(VMC_FULL_MASK, S.a[1][i].x, sl);
+    const float y1 = __shfl_sync(VMC_FULL_MASK, S.a[1][i].y, sl);
+    S.a[0][i] = s1 ? make_float2(x1, y1) : make_float2(x0, y0);
   }
   return src;
-}
-
-// Pivot key over the compacted layout (slot 0 holds original row orow).
-__device__ __forceinline__ unsigned lu_pivot_key_c(const LuRegs<64>& S, int orow) {
-  unsigned key = 0;
-  if ((S.U >> orow) & 1ull) key = (__float_as_uint(fabsf(S.a[0][0])) & ~63u) | (unsigned)(63 - orow);
-  return __reduce_max_sync(VMC_FULL_MASK, key);
-}
-
-// 16 pivot steps over the compacted layout: as lu_phase with one row a lane;
-// the lane holding pivot row p is found by a ballot on the original rows.
-template <int W>
-__device__ __forceinline__ void lu_phase_c(LuRegs<64>& S, float* prow, int lane, int orow) {
-#pragma unroll 1
-  for (int t = 0; t < 16; ++t) {
-    const unsigned key = S.key;
-    const int p = 63 - (int)(key & 63u);
-    const float best = __uint_as_float(key & ~63u);
-    if (orow == p) {
-#pragma unroll
-      for (int q = 0; q < W / 4; ++q)
-        reinterpret_cast<float4*>(prow)[q] =
-            make_float4(S.a[0][4 * q], S.a[0][4 * q + 1], S.a[0][4 * q + 2], S.a[0][4 * q + 3]);
-    }
-    __syncwarp();
-    float pv = prow[0];
-    const bool pvalid = key != 0u && (best > 0.0f) && isfinite(best);
-    if (!pvalid) { S.ok = false; pv = 1.0f; }
-    S.neg ^= (pv < 0.0f);
-    S.neg ^= __popcll(S.U & ((1ull << p) - 1ull)) & 1;
-    S.U &= ~(1ull << p);
-    const float m = S.mant * fabsf(pv);
-    const unsigned mb = __float_as_uint(m);
-    S.expo += (int)((mb >> 23) & 255u) - 127;
-    S.mant = __uint_as_float((mb & 0x007FFFFFu) | 0x3F800000u);
-    const float ipv = __frcp_rn(pv);
-    float pr[W];
-#pragma unroll
-    for (int q = 0; q < W / 4; ++q) {
-      const float4 t4 = reinterpret_cast<const float4*>(prow)[q];
-      pr[4 * q] = t4.x; pr[4 * q + 1] = t4.y; pr[4 * q + 2] = t4.z; pr[4 * q + 3] = t4.w;
-    }
-    const float f = S.a[0][0] * ipv;
-    S.a[0][0] = fmaf(-f, pr[1], S.a[0][1]);
-    S.key = lu_pivot_key_c(S, orow);
-#pragma unroll
-    for (int c = 2; c < W; ++c) S.a[0][c - 1] = fmaf(-f, pr[c], S.a[0][c]);
-    __syncwarp();
-  }
 }
 
 template <int NF>
@@ -730,7 +754,8 @@ __device__ __forceinline__ Det warp_logdet_f32(const float* __restrict__ A, floa
 #pragma unroll
     for (int q = 0; q < NF / 4; ++q) {
       float4 t = src[q];
-      S.a[r][4 * q] = t.x; S.a[r][4 * q + 1] = t.y; S.a[r][4 * q + 2] = t.z; S.a[r][4 * q + 3] = t.w;
+      S.a[r][2 * q] = make_float2(t.x, t.y);
+      S.a[r][2 * q + 1] = make_float2(t.z, t.w);
     }
   }
   S.U = (NF == 64) ? ~0ull : ((1ull << NF) - 1ull);
@@ -738,13 +763,13 @@ __device__ __forceinline__ Det warp_logdet_f32(const float* __restrict__ A, floa
   S.expo = 0;
   S.neg = 0;
   S.ok = true;
-  S.key = lu_pivot_key<NF>(S, lane);
-  lu_phase<NF, NF>(S, prow, lane);
-  lu_phase<NF, NF - 16>(S, prow, lane);
+  S.key = lu_pivot_key<NF, R, 0, 0, false>(S, lane, 0);
+  lu_phase<NF, R, NF, false>(S, prow, lane, 0);
+  lu_phase<NF, R, NF - 16, false>(S, prow, lane, 0);
   if constexpr (NF == 64) {
     const int orow = lu_compact<32>(S, lane);
-    lu_phase_c<32>(S, prow, lane, orow);
-    lu_phase_c<16>(S, prow, lane, orow);
+    lu_phase<64, 1, 32, true>(S, prow, lane, orow);   // slot 0 only from here on
+    lu_phase<64, 1, 16, true>(S, prow, lane, orow);
   }
   Det d;
   if (S.ok) {
@@ -843,7 +868,7 @@ struct LdArgs {
 };
 
 template <typename T, int NF, int MODE>
-__global__ void k_logdet(int64_t R, int64_t row0, int nf, const T* __restrict__ A, LdArgs la) {
+__global__ void __launch_bounds__(128, LU_MIN_CTAS) k_logdet(int64_t R, int64_t row0, int nf, const T* __restrict__ A, LdArgs la) {
   extern __shared__ __align__(16) uint8_t lsm[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t local = (int64_t)blockIdx.x * (blockDim.x >> 5) + warp;
