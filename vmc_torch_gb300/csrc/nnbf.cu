@@ -575,7 +575,8 @@ struct LuRegs {
   float mant;
   int expo, neg;
   bool ok;
-  unsigned key;  // pivot key of the next step (computed one step ahead)
+  unsigned key;   // pivot key of the next step (computed one step ahead)
+  uint64_t obit;  // compacted layout: bit of the original row held by the lane
 };
 
 // Resident 4-warp CTAs per SM that the LU kernel's register budget is held
@@ -595,7 +596,10 @@ __device__ __forceinline__ unsigned lu_pivot_key(const LuRegs<NF>& S, int lane, 
 #pragma unroll
   for (int r = 0; r < R; ++r) {
     const int row = COMPACT ? orow : lane + 32 * r;
-    if ((S.U >> row) & 1ull) {
+    // live test: 32-bit word of the lane's row, or the precomputed bit
+    const bool live = COMPACT ? (S.U & S.obit) != 0ull
+                              : ((((r == 0) ? (unsigned)S.U : (unsigned)(S.U >> 32)) >> lane) & 1u) != 0u;
+    if (live) {
       const unsigned kb = (__float_as_uint(fabsf(lu_el<E>(S.a[r][P]))) & ~63u) | (unsigned)(63 - row);
       key = kb > key ? kb : key;
     }
@@ -619,7 +623,11 @@ __device__ __forceinline__ float lu_pivot_update(LuRegs<NF>& S, unsigned key, in
   const unsigned mb = __float_as_uint(m);
   S.expo += (int)((mb >> 23) & 255u) - 127;
   S.mant = __uint_as_float((mb & 0x007FFFFFu) | 0x3F800000u);
-  return __frcp_rn(pv);
+  // elimination multipliers only: the hardware reciprocal (relative error
+  // ~2^-23) is as accurate as the multiplier's own rounding; |det| uses pv
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(pv));
+  return r;
 }
 
 // Pivot row (H pairs of the owning lane's register row) -> shared memory.
@@ -672,10 +680,15 @@ __device__ __forceinline__ void lu_update_shift(float2 (*a)[NP], const float* pr
 }
 
 // One pivot step on column K (0 or 1) of a phase of width W.  The next pivot
-// column is updated first so that its key reduction overlaps the rest.
+// column is updated first so that its key reduction overlaps the rest.  The
+// pivot row goes through shared slot K of the warp's two 64-float slots: a
+// slot is rewritten two steps later, after every lane has passed the barrier
+// of the step in between, so one barrier per step orders both the write
+// before the reads and the reads before the next write.
 template <int NF, int R, int W, int K, bool COMPACT>
-__device__ __forceinline__ void lu_step(LuRegs<NF>& S, float* prow, int lane, int orow) {
+__device__ __forceinline__ void lu_step(LuRegs<NF>& S, float* prow2, int lane, int orow) {
   constexpr int H = W / 2;
+  float* prow = prow2 + 64 * K;
   const unsigned key = S.key;
   const int p = 63 - (int)(key & 63u);
   // pivot row -> shared memory (warp-uniform branch on the register row)
@@ -707,7 +720,6 @@ __device__ __forceinline__ void lu_step(LuRegs<NF>& S, float* prow, int lane, in
     S.key = lu_pivot_key<NF, R, 0, 0, COMPACT>(S, lane, orow);
     lu_update_shift<R, H>(S.a, prow, f);
   }
-  __syncwarp();
 }
 
 // 16 pivot steps of width W (COMPACT: one row a lane, see lu_compact).
@@ -763,11 +775,13 @@ __device__ __forceinline__ Det warp_logdet_f32(const float* __restrict__ A, floa
   S.expo = 0;
   S.neg = 0;
   S.ok = true;
+  S.obit = 0ull;
   S.key = lu_pivot_key<NF, R, 0, 0, false>(S, lane, 0);
   lu_phase<NF, R, NF, false>(S, prow, lane, 0);
   lu_phase<NF, R, NF - 16, false>(S, prow, lane, 0);
   if constexpr (NF == 64) {
     const int orow = lu_compact<32>(S, lane);
+    S.obit = 1ull << orow;
     lu_phase<64, 1, 32, true>(S, prow, lane, orow);   // slot 0 only from here on
     lu_phase<64, 1, 16, true>(S, prow, lane, orow);
   }
@@ -883,7 +897,7 @@ __global__ void __launch_bounds__(128, LU_MIN_CTAS) k_logdet(int64_t R, int64_t 
   }
   Det d;
   if constexpr (sizeof(T) == 4) {
-    float* prow = reinterpret_cast<float*>(lsm) + warp * 64;
+    float* prow = reinterpret_cast<float*>(lsm) + warp * 128;  // two pivot-row slots
     d = warp_logdet_f32<NF>(reinterpret_cast<const float*>(A) + (size_t)local * NF * NF, prow);
   } else {
     double* s = reinterpret_cast<double*>(lsm) + (size_t)warp * (64 * 65);
@@ -1178,7 +1192,7 @@ int launch_eval_rows(int prec, int64_t R, int N, int nf, const uint64_t* row_occ
     const int64_t CH = R < kChunkRows ? R : kChunkRows;
     const int64_t n_chunks = (R + CH - 1) / CH;
     const int wpb = 4;
-    const size_t lsmem = wpb * 64 * sizeof(float);
+    const size_t lsmem = wpb * 128 * sizeof(float);  // two pivot-row slots per warp
     // chunk pipeline (two A slots inside the R-row workspace) unless the
     // stages are being timed one by one
     ChunkPipe* pipe = (allow_pipe && n_chunks > 1 && !g_timer.acc) ? chunk_pipe() : nullptr;
