@@ -428,6 +428,11 @@ def run_gb300(args):
                 "algorithmic": "LU: (2/3) nf^3 FLOP per evaluated proposal (nf=64); GEMMs: 2*M*N*K",
                 "per_kernel": per_kernel,
                 "backflow_gemm_tflops": bf_flops / (stage_ms[2] / 1e3) / 1e12 if stage_ms[2] else None,
+                # per_kernel times come from a pass with the chunk pipeline and walker
+                # groups off (every launch alone on the GPU); in the timed steps the LU
+                # overlaps the GEMMs and the other groups' launches.  LU work completed
+                # per unit of step time:
+                "lu_tflops_in_step": lu_flops / args.steps / (total_ms / args.steps / 1e3) / 1e12,
                 "hidden_gemm_tflops": l1_flops / (stage_ms[1] / 1e3) / 1e12 if stage_ms[1] else None}
 
     # ---- end-to-end through the public API with host buffers ----

@@ -568,6 +568,12 @@ struct Det { double logabs; double sign; };
 // shifting step too, or unrolling four steps, raises the register count past
 // 168 (3 CTAs of 4 warps per SM) or the loop body's code size, and measured
 // slower end to end.
+// Register layouts of the elimination: LU_FULL = rows lane and lane + 32;
+// LU_COMPACT = one live row a lane (after lu_compact); LU_PAIRED = two
+// matrices a warp, lanes 16 h .. 16 h + 15 holding two live rows each of
+// matrix h (after lu_pair_tails).
+enum { LU_FULL = 0, LU_COMPACT = 1, LU_PAIRED = 2 };
+
 template <int NF>
 struct LuRegs {
   float2 a[NF / 32][NF / 2];
@@ -577,6 +583,11 @@ struct LuRegs {
   bool ok;
   unsigned key;   // pivot key of the next step (computed one step ahead)
   uint64_t obit;  // compacted layout: bit of the original row held by the lane
+  // paired layout: original rows of the two register rows, their bits, and
+  // the half (matrix) the lane works on
+  int prow_of[2];
+  uint64_t pbit[2];
+  int half;
 };
 
 // Resident 4-warp CTAs per SM that the LU kernel's register budget is held
@@ -588,21 +599,29 @@ template <int E> __device__ __forceinline__ float lu_el(const float2& v) { retur
 // key (|a| bits with the low 6 mantissa bits replaced by 63 - row: larger
 // magnitude wins, ties -> smaller row).  The 6 dropped bits only matter for
 // magnitudes equal to 2^-17 relative, where either choice is a valid pivot.
-// The pivot column is element E of pair P.  COMPACT: one row a lane, slot 0
-// holding original row orow.
-template <int NF, int R, int P, int E, bool COMPACT>
+// The pivot column is element E of pair P; LM is the register layout
+// (LU_COMPACT: slot 0 holds original row orow).  In the paired layout each
+// half reduces its own matrix's keys (two warp reductions, the other half's
+// keys masked to 0).
+template <int NF, int R, int P, int E, int LM>
 __device__ __forceinline__ unsigned lu_pivot_key(const LuRegs<NF>& S, int lane, int orow) {
   unsigned key = 0;
 #pragma unroll
   for (int r = 0; r < R; ++r) {
-    const int row = COMPACT ? orow : lane + 32 * r;
+    const int row = LM == LU_COMPACT ? orow : LM == LU_PAIRED ? S.prow_of[r] : lane + 32 * r;
     // live test: 32-bit word of the lane's row, or the precomputed bit
-    const bool live = COMPACT ? (S.U & S.obit) != 0ull
-                              : ((((r == 0) ? (unsigned)S.U : (unsigned)(S.U >> 32)) >> lane) & 1u) != 0u;
+    const bool live = LM == LU_COMPACT ? (S.U & S.obit) != 0ull
+                      : LM == LU_PAIRED ? (S.U & S.pbit[r]) != 0ull
+                                        : ((((r == 0) ? (unsigned)S.U : (unsigned)(S.U >> 32)) >> lane) & 1u) != 0u;
     if (live) {
       const unsigned kb = (__float_as_uint(fabsf(lu_el<E>(S.a[r][P]))) & ~63u) | (unsigned)(63 - row);
       key = kb > key ? kb : key;
     }
+  }
+  if constexpr (LM == LU_PAIRED) {
+    const unsigned k0 = __reduce_max_sync(VMC_FULL_MASK, S.half ? 0u : key);
+    const unsigned k1 = __reduce_max_sync(VMC_FULL_MASK, S.half ? key : 0u);
+    return S.half ? k1 : k0;
   }
   return __reduce_max_sync(VMC_FULL_MASK, key);
 }
@@ -685,15 +704,19 @@ __device__ __forceinline__ void lu_update_shift(float2 (*a)[NP], const float* pr
 // slot is rewritten two steps later, after every lane has passed the barrier
 // of the step in between, so one barrier per step orders both the write
 // before the reads and the reads before the next write.
-template <int NF, int R, int W, int K, bool COMPACT>
+template <int NF, int R, int W, int K, int LM>
 __device__ __forceinline__ void lu_step(LuRegs<NF>& S, float* prow2, int lane, int orow) {
   constexpr int H = W / 2;
-  float* prow = prow2 + 64 * K;
+  // paired layout: each half's pivot row in its own 32-float part of the slot
+  float* prow = prow2 + 64 * K + (LM == LU_PAIRED ? 32 * S.half : 0);
   const unsigned key = S.key;
   const int p = 63 - (int)(key & 63u);
   // pivot row -> shared memory (warp-uniform branch on the register row)
-  if (COMPACT) {
+  if (LM == LU_COMPACT) {
     if (orow == p) lu_store_row<H>(S.a[0], prow);
+  } else if (LM == LU_PAIRED) {
+    if (S.prow_of[0] == p) lu_store_row<H>(S.a[0], prow);
+    else if (S.prow_of[1] == p) lu_store_row<H>(S.a[R - 1], prow);
   } else if (R > 1 && (p >> 5)) {
     if ((p & 31) == lane) lu_store_row<H>(S.a[R - 1], prow);
   } else {
@@ -708,7 +731,7 @@ __device__ __forceinline__ void lu_step(LuRegs<NF>& S, float* prow2, int lane, i
     const float pn = prow[1];
 #pragma unroll
     for (int r = 0; r < R; ++r) S.a[r][0].y = fmaf(-f[r], pn, S.a[r][0].y);
-    S.key = lu_pivot_key<NF, R, 0, 1, COMPACT>(S, lane, orow);
+    S.key = lu_pivot_key<NF, R, 0, 1, LM>(S, lane, orow);
     lu_update_inplace<R, H>(S.a, prow, f);
   } else {
     const float2 pn = reinterpret_cast<const float2*>(prow)[1];
@@ -717,18 +740,18 @@ __device__ __forceinline__ void lu_step(LuRegs<NF>& S, float* prow2, int lane, i
       S.a[r][0].x = fmaf(-f[r], pn.x, S.a[r][1].x);
       S.a[r][0].y = fmaf(-f[r], pn.y, S.a[r][1].y);
     }
-    S.key = lu_pivot_key<NF, R, 0, 0, COMPACT>(S, lane, orow);
+    S.key = lu_pivot_key<NF, R, 0, 0, LM>(S, lane, orow);
     lu_update_shift<R, H>(S.a, prow, f);
   }
 }
 
-// 16 pivot steps of width W (COMPACT: one row a lane, see lu_compact).
-template <int NF, int R, int W, bool COMPACT>
+// 16 pivot steps of width W in register layout LM.
+template <int NF, int R, int W, int LM>
 __device__ __forceinline__ void lu_phase(LuRegs<NF>& S, float* prow, int lane, int orow) {
 #pragma unroll 1
   for (int t = 0; t < 8; ++t) {
-    lu_step<NF, R, W, 0, COMPACT>(S, prow, lane, orow);
-    lu_step<NF, R, W, 1, COMPACT>(S, prow, lane, orow);
+    lu_step<NF, R, W, 0, LM>(S, prow, lane, orow);
+    lu_step<NF, R, W, 1, LM>(S, prow, lane, orow);
   }
 }
 
@@ -755,11 +778,8 @@ __device__ __forceinline__ int lu_compact(LuRegs<64>& S, int lane) {
 }
 
 template <int NF>
-__device__ __forceinline__ Det warp_logdet_f32(const float* __restrict__ A, float* prow) {
-  static_assert(NF == 32 || NF == 64, "NF must be 32 or 64");
+__device__ __forceinline__ void lu_load(LuRegs<NF>& S, const float* __restrict__ A, int lane) {
   constexpr int R = NF / 32;
-  const int lane = threadIdx.x & 31;
-  LuRegs<NF> S;
 #pragma unroll
   for (int r = 0; r < R; ++r) {
     const float4* src = reinterpret_cast<const float4*>(A + (size_t)(lane + 32 * r) * NF);
@@ -776,26 +796,113 @@ __device__ __forceinline__ Det warp_logdet_f32(const float* __restrict__ A, floa
   S.neg = 0;
   S.ok = true;
   S.obit = 0ull;
-  S.key = lu_pivot_key<NF, R, 0, 0, false>(S, lane, 0);
-  lu_phase<NF, R, NF, false>(S, prow, lane, 0);
-  lu_phase<NF, R, NF - 16, false>(S, prow, lane, 0);
-  if constexpr (NF == 64) {
-    const int orow = lu_compact<32>(S, lane);
-    S.obit = 1ull << orow;
-    lu_phase<64, 1, 32, true>(S, prow, lane, orow);   // slot 0 only from here on
-    lu_phase<64, 1, 16, true>(S, prow, lane, orow);
-  }
+  S.key = lu_pivot_key<NF, R, 0, 0, LU_FULL>(S, lane, 0);
+}
+
+__device__ __forceinline__ Det lu_det(bool ok, float mant, int expo, int neg) {
   Det d;
-  if (S.ok) {
+  if (ok) {
     // mantissa in [1, 2): FP32 log is accurate to ~1e-7 absolute; the exponent
     // part is exact; only the final sum is FP64 (FP64 pipes are scarce on GB300)
-    d.logabs = (double)logf(S.mant) + (double)S.expo * 0.69314718055994530942;
-    d.sign = S.neg ? -1.0 : 1.0;
+    d.logabs = (double)logf(mant) + (double)expo * 0.69314718055994530942;
+    d.sign = neg ? -1.0 : 1.0;
   } else {
     d.logabs = -INFINITY;
     d.sign = 0.0;
   }
   return d;
+}
+
+template <int NF>
+__device__ __forceinline__ Det warp_logdet_f32(const float* __restrict__ A, float* prow) {
+  static_assert(NF == 32 || NF == 64, "NF must be 32 or 64");
+  constexpr int R = NF / 32;
+  const int lane = threadIdx.x & 31;
+  LuRegs<NF> S;
+  lu_load<NF>(S, A, lane);
+  lu_phase<NF, R, NF, LU_FULL>(S, prow, lane, 0);
+  lu_phase<NF, R, NF - 16, LU_FULL>(S, prow, lane, 0);
+  if constexpr (NF == 64) {
+    const int orow = lu_compact<32>(S, lane);
+    S.obit = 1ull << orow;
+    lu_phase<64, 1, 32, LU_COMPACT>(S, prow, lane, orow);   // slot 0 only from here on
+    lu_phase<64, 1, 16, LU_COMPACT>(S, prow, lane, orow);
+  }
+  return lu_det(S.ok, S.mant, S.expo, S.neg);
+}
+
+// Two 64 x 64 matrices on one warp.  Each runs its first 32 pivot steps in
+// the full layout, then parks its 32 x 32 remainder in its own first 4 KB
+// (L2; the warp has consumed those rows) and its scalar state in the warp's
+// shared words, so nothing but indices stays live from one matrix to the
+// next.  The remainders then share the warp: half h (lanes 16 h .. 16 h + 15)
+// reloads live rows i and i + 16 of matrix h, and the last 32 steps of both
+// run as one instruction stream.  Pivot choices and arithmetic equal the
+// one-matrix path's, so the results are bit-identical to it.  The matrices
+// are rows sw[38 + h] of A; with nm = 1 both halves carry matrix 0 and the
+// second result is unused.
+__device__ __forceinline__ void warp_logdet_f32_pair(float* A, float* prow, uint32_t* sw, int nm, Det& d0,
+                                                     Det& d1) {
+  const int lane = threadIdx.x & 31;
+  LuRegs<64> S;
+#pragma unroll 1
+  for (int m = 0; m < nm; ++m) {
+    float* Am = A + (size_t)sw[38 + m] * 4096;
+    lu_load<64>(S, Am, lane);
+    lu_phase<64, 2, 64, LU_FULL>(S, prow, lane, 0);
+    lu_phase<64, 2, 48, LU_FULL>(S, prow, lane, 0);
+    const int orow = lu_compact<32>(S, lane);
+    __syncwarp();  // every lane's loads of the matrix precede the parking stores
+    float4* park = reinterpret_cast<float4*>(Am);
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+      __stcg(park + q * 32 + lane,
+             make_float4(S.a[0][2 * q].x, S.a[0][2 * q].y, S.a[0][2 * q + 1].x, S.a[0][2 * q + 1].y));
+    uint32_t* w = sw + 40 * m;   // [0, 32): original row held by each lane; [32, 37): scalar state
+    w[lane] = (uint32_t)orow;
+    if (lane == 0) {
+      w[32] = (uint32_t)S.U;
+      w[33] = (uint32_t)(S.U >> 32);
+      w[34] = __float_as_uint(S.mant);
+      w[35] = (uint32_t)S.expo;
+      w[36] = (uint32_t)S.neg | ((uint32_t)S.ok << 1);
+    }
+  }
+  __syncwarp();  // parked rows and words visible to every lane
+  const int half = lane >> 4;
+  const int h = nm == 2 ? half : 0;   // matrix carried by this lane
+  const int i = lane & 15;
+  const uint32_t* w = sw + 40 * h;
+  const float4* park = reinterpret_cast<const float4*>(A + (size_t)sw[38 + h] * 4096);
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const float4 v0 = __ldcg(park + q * 32 + i), v1 = __ldcg(park + q * 32 + i + 16);
+    S.a[0][2 * q] = make_float2(v0.x, v0.y);
+    S.a[0][2 * q + 1] = make_float2(v0.z, v0.w);
+    S.a[1][2 * q] = make_float2(v1.x, v1.y);
+    S.a[1][2 * q + 1] = make_float2(v1.z, v1.w);
+  }
+  S.prow_of[0] = (int)w[i];
+  S.prow_of[1] = (int)w[i + 16];
+  S.U = (uint64_t)w[32] | ((uint64_t)w[33] << 32);
+  S.mant = __uint_as_float(w[34]);
+  S.expo = (int)w[35];
+  S.neg = (int)(w[36] & 1u);
+  S.ok = (w[36] >> 1) & 1u;
+  S.half = half;
+  S.pbit[0] = 1ull << S.prow_of[0];
+  S.pbit[1] = 1ull << S.prow_of[1];
+  S.key = lu_pivot_key<64, 2, 0, 0, LU_PAIRED>(S, lane, 0);
+  lu_phase<64, 2, 32, LU_PAIRED>(S, prow, lane, 0);
+  lu_phase<64, 2, 16, LU_PAIRED>(S, prow, lane, 0);
+  // each half's state -> both results
+  const float mo = __shfl_xor_sync(VMC_FULL_MASK, S.mant, 16);
+  const int eo = __shfl_xor_sync(VMC_FULL_MASK, S.expo, 16);
+  const int no = __shfl_xor_sync(VMC_FULL_MASK, S.neg, 16);
+  const bool oo = __shfl_xor_sync(VMC_FULL_MASK, (int)S.ok, 16) != 0;
+  const Det mine = lu_det(S.ok, S.mant, S.expo, S.neg), other = lu_det(oo, mo, eo, no);
+  d0 = half ? other : mine;
+  d1 = half ? mine : other;
 }
 
 // FP64 in shared memory (nf <= 64 at run time), same retired-row scheme.
@@ -881,28 +988,11 @@ struct LdArgs {
   double* term;
 };
 
-template <typename T, int NF, int MODE>
-__global__ void __launch_bounds__(128, LU_MIN_CTAS) k_logdet(int64_t R, int64_t row0, int nf, const T* __restrict__ A, LdArgs la) {
-  extern __shared__ __align__(16) uint8_t lsm[];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t local = (int64_t)blockIdx.x * (blockDim.x >> 5) + warp;
-  if (local >= R) return;
-  const int64_t row = row0 + local;
-  if (MODE == LD_ACCEPT) {
-    if (!la.rec[row].flag) return;
-    if (la.n_eval && lane == 0) atomicAdd(la.n_eval, 1ull);
-  }
-  if (MODE == LD_ACCEPT_Q) {
-    if (!la.rec4[row].flag) return;
-  }
-  Det d;
-  if constexpr (sizeof(T) == 4) {
-    float* prow = reinterpret_cast<float*>(lsm) + warp * 128;  // two pivot-row slots
-    d = warp_logdet_f32<NF>(reinterpret_cast<const float*>(A) + (size_t)local * NF * NF, prow);
-  } else {
-    double* s = reinterpret_cast<double*>(lsm) + (size_t)warp * (64 * 65);
-    d = warp_logdet_f64(reinterpret_cast<const double*>(A) + (size_t)local * nf * nf, nf, s);
-  }
+// What the evaluated row's log-determinant is used for: EVAL stores it, ELOC
+// forms the hop term, ACCEPT / ACCEPT_Q run the Metropolis(-Hastings) test and
+// apply an accepted move (whole warp).
+template <typename T, int MODE>
+__device__ __forceinline__ void ld_finish(int64_t row, const Det& d, const LdArgs& la, int lane) {
   if (MODE == LD_EVAL) {
     if (lane == 0) { la.sign[row] = d.sign; la.logabs[row] = d.logabs; }
   } else if (MODE == LD_ELOC) {
@@ -966,6 +1056,69 @@ __global__ void __launch_bounds__(128, LU_MIN_CTAS) k_logdet(int64_t R, int64_t 
       }
     }
   }
+}
+
+template <typename T, int NF, int MODE>
+__global__ void __launch_bounds__(128, LU_MIN_CTAS) k_logdet(int64_t R, int64_t row0, int nf, const T* __restrict__ A, LdArgs la) {
+  extern __shared__ __align__(16) uint8_t lsm[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t local = (int64_t)blockIdx.x * (blockDim.x >> 5) + warp;
+  if (local >= R) return;
+  const int64_t row = row0 + local;
+  if (MODE == LD_ACCEPT) {
+    if (!la.rec[row].flag) return;
+    if (la.n_eval && lane == 0) atomicAdd(la.n_eval, 1ull);
+  }
+  if (MODE == LD_ACCEPT_Q) {
+    if (!la.rec4[row].flag) return;
+  }
+  Det d;
+  if constexpr (sizeof(T) == 4) {
+    float* prow = reinterpret_cast<float*>(lsm) + warp * 128;  // two pivot-row slots
+    d = warp_logdet_f32<NF>(reinterpret_cast<const float*>(A) + (size_t)local * NF * NF, prow);
+  } else {
+    double* s = reinterpret_cast<double*>(lsm) + (size_t)warp * (64 * 65);
+    d = warp_logdet_f64(reinterpret_cast<const double*>(A) + (size_t)local * nf * nf, nf, s);
+  }
+  ld_finish<T, MODE>(row, d, la, lane);
+}
+
+template <int MODE>
+__device__ __forceinline__ bool ld_flag(const LdArgs& la, int64_t row) {
+  if (MODE == LD_ACCEPT) return la.rec[row].flag != 0;
+  if (MODE == LD_ACCEPT_Q) return la.rec4[row].flag != 0;
+  return true;
+}
+
+// FP32 64 x 64 rows, two matrices a warp: a CTA of 4 warps takes 8 rows,
+// keeps those that need an evaluation and hands them out in pairs (warp w:
+// the (2w)-th and (2w+1)-th; at most one warp of a CTA is left with one).
+// Shared memory per warp: 128 floats of pivot-row slots + 2 x 40 words.
+constexpr int LDP_WARP_WORDS = 128 + 80;
+template <int MODE>
+__global__ void __launch_bounds__(128, LU_MIN_CTAS) k_logdet_pair(int64_t R, int64_t row0, float* A, LdArgs la) {
+  extern __shared__ __align__(16) uint8_t lsm[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t base = (int64_t)blockIdx.x * 8;
+  bool fl = false;
+  if (lane < 8 && base + lane < R) fl = ld_flag<MODE>(la, row0 + base + lane);
+  unsigned m = __ballot_sync(VMC_FULL_MASK, fl);
+  for (int i = 0; i < 2 * warp; ++i) m &= m - 1u;
+  if (!m) return;
+  const int64_t l0 = base + (__ffs(m) - 1);
+  m &= m - 1u;
+  const int64_t l1 = m ? base + (__ffs(m) - 1) : -1;
+  if (MODE == LD_ACCEPT && la.n_eval && lane == 0) atomicAdd(la.n_eval, l1 >= 0 ? 2ull : 1ull);
+  float* prow = reinterpret_cast<float*>(lsm) + warp * LDP_WARP_WORDS;
+  uint32_t* sw = reinterpret_cast<uint32_t*>(prow + 128);
+  // the rows (local indices < 2^31) wait in shared memory during the elimination
+  if (lane == 0) { sw[38] = (uint32_t)l0; sw[39] = (uint32_t)(l1 < 0 ? l0 : l1); }
+  const int nd = l1 < 0 ? 1 : 2;
+  __syncwarp();
+  Det d0, d1;
+  warp_logdet_f32_pair(A, prow, sw, nd, d0, d1);
+#pragma unroll 1
+  for (int k = 0; k < nd; ++k) ld_finish<float, MODE>(row0 + (int64_t)sw[38 + k], k ? d1 : d0, la, lane);
 }
 
 // per-walker local energy: U * doublons + segmented sum of the hop terms
@@ -1224,11 +1377,13 @@ int launch_eval_rows(int prec, int64_t R, int N, int nf, const uint64_t* row_occ
       }
       STAGE_BEGIN(3);
       const unsigned gl = (unsigned)((Rc + wpb - 1) / wpb);
-      if (nf == 64) {
-        if (ldmode == LD_ACCEPT) k_logdet<float, 64, LD_ACCEPT><<<gl, 32 * wpb, lsmem, st>>>(Rc, c0, nf, Ac, la);
-        else if (ldmode == LD_EVAL) k_logdet<float, 64, LD_EVAL><<<gl, 32 * wpb, lsmem, st>>>(Rc, c0, nf, Ac, la);
-        else if (ldmode == LD_ACCEPT_Q) k_logdet<float, 64, LD_ACCEPT_Q><<<gl, 32 * wpb, lsmem, st>>>(Rc, c0, nf, Ac, la);
-        else k_logdet<float, 64, LD_ELOC><<<gl, 32 * wpb, lsmem, st>>>(Rc, c0, nf, Ac, la);
+      if (nf == 64) {  // two rows a warp (the orbital-matrix slot is scratch: the LU parks in it)
+        const unsigned gp = (unsigned)((Rc + 2 * wpb - 1) / (2 * wpb));
+        const size_t psmem = (size_t)wpb * LDP_WARP_WORDS * sizeof(float);
+        if (ldmode == LD_ACCEPT) k_logdet_pair<LD_ACCEPT><<<gp, 32 * wpb, psmem, st>>>(Rc, c0, Ac, la);
+        else if (ldmode == LD_EVAL) k_logdet_pair<LD_EVAL><<<gp, 32 * wpb, psmem, st>>>(Rc, c0, Ac, la);
+        else if (ldmode == LD_ACCEPT_Q) k_logdet_pair<LD_ACCEPT_Q><<<gp, 32 * wpb, psmem, st>>>(Rc, c0, Ac, la);
+        else k_logdet_pair<LD_ELOC><<<gp, 32 * wpb, psmem, st>>>(Rc, c0, Ac, la);
       } else {
         if (ldmode == LD_ACCEPT) k_logdet<float, 32, LD_ACCEPT><<<gl, 32 * wpb, lsmem, st>>>(Rc, c0, nf, Ac, la);
         else if (ldmode == LD_EVAL) k_logdet<float, 32, LD_EVAL><<<gl, 32 * wpb, lsmem, st>>>(Rc, c0, nf, Ac, la);
