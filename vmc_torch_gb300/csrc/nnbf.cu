@@ -568,11 +568,11 @@ struct Det { double logabs; double sign; };
 // shifting step too, or unrolling four steps, raises the register count past
 // 168 (3 CTAs of 4 warps per SM) or the loop body's code size, and measured
 // slower end to end.
-// Register layouts of the elimination: LU_FULL = rows lane and lane + 32;
-// LU_COMPACT = one live row a lane (after lu_compact); LU_PAIRED = two
-// matrices a warp, lanes 16 h .. 16 h + 15 holding two live rows each of
-// matrix h (after lu_pair_tails).
-enum { LU_FULL = 0, LU_COMPACT = 1, LU_PAIRED = 2 };
+// Register layouts of the elimination: LU_FULL = rows lane and lane + 32 (of
+// a 64-row matrix; row lane of a 32-row one); LU_PAIRED = two matrices a
+// warp, lanes 16 h .. 16 h + 15 holding two live rows each of matrix h (see
+// warp_logdet_f32_pair).
+enum { LU_FULL = 0, LU_PAIRED = 1 };
 
 template <int NF>
 struct LuRegs {
@@ -582,7 +582,6 @@ struct LuRegs {
   int expo, neg;
   bool ok;
   unsigned key;   // pivot key of the next step (computed one step ahead)
-  uint64_t obit;  // compacted layout: bit of the original row held by the lane
   // paired layout: original rows of the two register rows, their bits, and
   // the half (matrix) the lane works on
   int prow_of[2];
@@ -599,20 +598,18 @@ template <int E> __device__ __forceinline__ float lu_el(const float2& v) { retur
 // key (|a| bits with the low 6 mantissa bits replaced by 63 - row: larger
 // magnitude wins, ties -> smaller row).  The 6 dropped bits only matter for
 // magnitudes equal to 2^-17 relative, where either choice is a valid pivot.
-// The pivot column is element E of pair P; LM is the register layout
-// (LU_COMPACT: slot 0 holds original row orow).  In the paired layout each
-// half reduces its own matrix's keys (two warp reductions, the other half's
-// keys masked to 0).
+// The pivot column is element E of pair P; LM is the register layout.  In
+// the paired layout each half reduces its own matrix's keys (two warp
+// reductions, the other half's keys masked to 0).
 template <int NF, int R, int P, int E, int LM>
-__device__ __forceinline__ unsigned lu_pivot_key(const LuRegs<NF>& S, int lane, int orow) {
+__device__ __forceinline__ unsigned lu_pivot_key(const LuRegs<NF>& S, int lane) {
   unsigned key = 0;
 #pragma unroll
   for (int r = 0; r < R; ++r) {
-    const int row = LM == LU_COMPACT ? orow : LM == LU_PAIRED ? S.prow_of[r] : lane + 32 * r;
-    // live test: 32-bit word of the lane's row, or the precomputed bit
-    const bool live = LM == LU_COMPACT ? (S.U & S.obit) != 0ull
-                      : LM == LU_PAIRED ? (S.U & S.pbit[r]) != 0ull
-                                        : ((((r == 0) ? (unsigned)S.U : (unsigned)(S.U >> 32)) >> lane) & 1u) != 0u;
+    const int row = LM == LU_PAIRED ? S.prow_of[r] : lane + 32 * r;
+    // live test: the precomputed bit, or the 32-bit word of the lane's row
+    const bool live = LM == LU_PAIRED ? (S.U & S.pbit[r]) != 0ull
+                                      : ((((r == 0) ? (unsigned)S.U : (unsigned)(S.U >> 32)) >> lane) & 1u) != 0u;
     if (live) {
       const unsigned kb = (__float_as_uint(fabsf(lu_el<E>(S.a[r][P]))) & ~63u) | (unsigned)(63 - row);
       key = kb > key ? kb : key;
@@ -705,16 +702,14 @@ __device__ __forceinline__ void lu_update_shift(float2 (*a)[NP], const float* pr
 // of the step in between, so one barrier per step orders both the write
 // before the reads and the reads before the next write.
 template <int NF, int R, int W, int K, int LM>
-__device__ __forceinline__ void lu_step(LuRegs<NF>& S, float* prow2, int lane, int orow) {
+__device__ __forceinline__ void lu_step(LuRegs<NF>& S, float* prow2, int lane) {
   constexpr int H = W / 2;
   // paired layout: each half's pivot row in its own 32-float part of the slot
   float* prow = prow2 + 64 * K + (LM == LU_PAIRED ? 32 * S.half : 0);
   const unsigned key = S.key;
   const int p = 63 - (int)(key & 63u);
   // pivot row -> shared memory (warp-uniform branch on the register row)
-  if (LM == LU_COMPACT) {
-    if (orow == p) lu_store_row<H>(S.a[0], prow);
-  } else if (LM == LU_PAIRED) {
+  if (LM == LU_PAIRED) {
     if (S.prow_of[0] == p) lu_store_row<H>(S.a[0], prow);
     else if (S.prow_of[1] == p) lu_store_row<H>(S.a[R - 1], prow);
   } else if (R > 1 && (p >> 5)) {
@@ -731,7 +726,7 @@ __device__ __forceinline__ void lu_step(LuRegs<NF>& S, float* prow2, int lane, i
     const float pn = prow[1];
 #pragma unroll
     for (int r = 0; r < R; ++r) S.a[r][0].y = fmaf(-f[r], pn, S.a[r][0].y);
-    S.key = lu_pivot_key<NF, R, 0, 1, LM>(S, lane, orow);
+    S.key = lu_pivot_key<NF, R, 0, 1, LM>(S, lane);
     lu_update_inplace<R, H>(S.a, prow, f);
   } else {
     const float2 pn = reinterpret_cast<const float2*>(prow)[1];
@@ -740,25 +735,25 @@ __device__ __forceinline__ void lu_step(LuRegs<NF>& S, float* prow2, int lane, i
       S.a[r][0].x = fmaf(-f[r], pn.x, S.a[r][1].x);
       S.a[r][0].y = fmaf(-f[r], pn.y, S.a[r][1].y);
     }
-    S.key = lu_pivot_key<NF, R, 0, 0, LM>(S, lane, orow);
+    S.key = lu_pivot_key<NF, R, 0, 0, LM>(S, lane);
     lu_update_shift<R, H>(S.a, prow, f);
   }
 }
 
 // 16 pivot steps of width W in register layout LM.
 template <int NF, int R, int W, int LM>
-__device__ __forceinline__ void lu_phase(LuRegs<NF>& S, float* prow, int lane, int orow) {
+__device__ __forceinline__ void lu_phase(LuRegs<NF>& S, float* prow, int lane) {
 #pragma unroll 1
   for (int t = 0; t < 8; ++t) {
-    lu_step<NF, R, W, 0, LM>(S, prow, lane, orow);
-    lu_step<NF, R, W, 1, LM>(S, prow, lane, orow);
+    lu_step<NF, R, W, 0, LM>(S, prow, lane);
+    lu_step<NF, R, W, 1, LM>(S, prow, lane);
   }
 }
 
 // After 32 pivot steps of a 64-row matrix exactly 32 rows are retired.  The
 // live rows move into register slot 0, one per lane in ascending row order
-// (lane L takes the L-th live row), so that the last 32 steps update one row
-// per lane instead of two.  Returns the original row now held by the lane.
+// (lane L takes the L-th live row), ready to be parked and regrouped into the
+// paired layout.  Returns the original row now held by the lane.
 template <int W>
 __device__ __forceinline__ int lu_compact(LuRegs<64>& S, int lane) {
   uint64_t m = S.U;
@@ -795,8 +790,7 @@ __device__ __forceinline__ void lu_load(LuRegs<NF>& S, const float* __restrict__
   S.expo = 0;
   S.neg = 0;
   S.ok = true;
-  S.obit = 0ull;
-  S.key = lu_pivot_key<NF, R, 0, 0, LU_FULL>(S, lane, 0);
+  S.key = lu_pivot_key<NF, R, 0, 0, LU_FULL>(S, lane);
 }
 
 __device__ __forceinline__ Det lu_det(bool ok, float mant, int expo, int neg) {
@@ -813,21 +807,16 @@ __device__ __forceinline__ Det lu_det(bool ok, float mant, int expo, int neg) {
   return d;
 }
 
+// One 32 x 32 matrix a warp (64 x 64 matrices go two a warp through
+// warp_logdet_f32_pair).
 template <int NF>
 __device__ __forceinline__ Det warp_logdet_f32(const float* __restrict__ A, float* prow) {
-  static_assert(NF == 32 || NF == 64, "NF must be 32 or 64");
-  constexpr int R = NF / 32;
+  static_assert(NF == 32, "one-matrix path: NF = 32");
   const int lane = threadIdx.x & 31;
   LuRegs<NF> S;
   lu_load<NF>(S, A, lane);
-  lu_phase<NF, R, NF, LU_FULL>(S, prow, lane, 0);
-  lu_phase<NF, R, NF - 16, LU_FULL>(S, prow, lane, 0);
-  if constexpr (NF == 64) {
-    const int orow = lu_compact<32>(S, lane);
-    S.obit = 1ull << orow;
-    lu_phase<64, 1, 32, LU_COMPACT>(S, prow, lane, orow);   // slot 0 only from here on
-    lu_phase<64, 1, 16, LU_COMPACT>(S, prow, lane, orow);
-  }
+  lu_phase<NF, 1, NF, LU_FULL>(S, prow, lane);
+  lu_phase<NF, 1, NF - 16, LU_FULL>(S, prow, lane);
   return lu_det(S.ok, S.mant, S.expo, S.neg);
 }
 
@@ -837,8 +826,9 @@ __device__ __forceinline__ Det warp_logdet_f32(const float* __restrict__ A, floa
 // shared words, so nothing but indices stays live from one matrix to the
 // next.  The remainders then share the warp: half h (lanes 16 h .. 16 h + 15)
 // reloads live rows i and i + 16 of matrix h, and the last 32 steps of both
-// run as one instruction stream.  Pivot choices and arithmetic equal the
-// one-matrix path's, so the results are bit-identical to it.  The matrices
+// run as one instruction stream.  A row's updates are the same FMAs in either
+// layout and the pivot keys carry the original row numbers, so a matrix's
+// result does not depend on its partner or on the pairing.  The matrices
 // are rows sw[38 + h] of A; with nm = 1 both halves carry matrix 0 and the
 // second result is unused.
 __device__ __forceinline__ void warp_logdet_f32_pair(float* A, float* prow, uint32_t* sw, int nm, Det& d0,
@@ -849,8 +839,8 @@ __device__ __forceinline__ void warp_logdet_f32_pair(float* A, float* prow, uint
   for (int m = 0; m < nm; ++m) {
     float* Am = A + (size_t)sw[38 + m] * 4096;
     lu_load<64>(S, Am, lane);
-    lu_phase<64, 2, 64, LU_FULL>(S, prow, lane, 0);
-    lu_phase<64, 2, 48, LU_FULL>(S, prow, lane, 0);
+    lu_phase<64, 2, 64, LU_FULL>(S, prow, lane);
+    lu_phase<64, 2, 48, LU_FULL>(S, prow, lane);
     const int orow = lu_compact<32>(S, lane);
     __syncwarp();  // every lane's loads of the matrix precede the parking stores
     float4* park = reinterpret_cast<float4*>(Am);
@@ -892,9 +882,9 @@ __device__ __forceinline__ void warp_logdet_f32_pair(float* A, float* prow, uint
   S.half = half;
   S.pbit[0] = 1ull << S.prow_of[0];
   S.pbit[1] = 1ull << S.prow_of[1];
-  S.key = lu_pivot_key<64, 2, 0, 0, LU_PAIRED>(S, lane, 0);
-  lu_phase<64, 2, 32, LU_PAIRED>(S, prow, lane, 0);
-  lu_phase<64, 2, 16, LU_PAIRED>(S, prow, lane, 0);
+  S.key = lu_pivot_key<64, 2, 0, 0, LU_PAIRED>(S, lane);
+  lu_phase<64, 2, 32, LU_PAIRED>(S, prow, lane);
+  lu_phase<64, 2, 16, LU_PAIRED>(S, prow, lane);
   // each half's state -> both results
   const float mo = __shfl_xor_sync(VMC_FULL_MASK, S.mant, 16);
   const int eo = __shfl_xor_sync(VMC_FULL_MASK, S.expo, 16);
