@@ -820,6 +820,70 @@ __device__ __forceinline__ Det warp_logdet_f32(const float* __restrict__ A, floa
   return lu_det(S.ok, S.mant, S.expo, S.neg);
 }
 
+// Last 32 pivot steps of a 64 x 64 matrix whose first 32 ran on this warp
+// (S after lu_compact, lane L holding live row L, orow its original row),
+// together with a partner matrix when one is given.  Partner (psw != null):
+// the 32 x 32 remainder parked at park (lane-major float4 rows) with its
+// original rows in psw[0..31] and scalar state in psw[32..36].  The warp
+// splits into halves: half 0 (lanes 0..15) carries live rows L and L + 16 of
+// the own matrix, half 1 those of the partner (or of the own matrix again if
+// there is none), and both tails run as one instruction stream.  A row's
+// updates are the same FMAs in every layout and the pivot keys carry the
+// original row numbers, so a matrix's result does not depend on its partner
+// or on the pairing.  d0: own matrix, d1: partner.
+__device__ __forceinline__ void lu_tail_pair(LuRegs<64>& S, int orow, const float4* park, const uint32_t* psw,
+                                             float* prow, Det& d0, Det& d1) {
+  const int lane = threadIdx.x & 31;
+  const int half = lane >> 4;
+  const int i = lane & 15;
+  float2 t[16];
+#pragma unroll
+  for (int k = 0; k < 16; ++k) t[k] = make_float2(__shfl_xor_sync(VMC_FULL_MASK, S.a[0][k].x, 16),
+                                                  __shfl_xor_sync(VMC_FULL_MASK, S.a[0][k].y, 16));
+  const int orow_x = __shfl_xor_sync(VMC_FULL_MASK, orow, 16);
+  if (half == 0) {
+#pragma unroll
+    for (int k = 0; k < 16; ++k) S.a[1][k] = t[k];
+    S.prow_of[0] = orow;
+    S.prow_of[1] = orow_x;
+  } else if (psw == nullptr) {
+#pragma unroll
+    for (int k = 0; k < 16; ++k) { S.a[1][k] = S.a[0][k]; S.a[0][k] = t[k]; }
+    S.prow_of[0] = orow_x;
+    S.prow_of[1] = orow;
+  } else {
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const float4 v0 = __ldcg(park + q * 32 + i), v1 = __ldcg(park + q * 32 + i + 16);
+      S.a[0][2 * q] = make_float2(v0.x, v0.y);
+      S.a[0][2 * q + 1] = make_float2(v0.z, v0.w);
+      S.a[1][2 * q] = make_float2(v1.x, v1.y);
+      S.a[1][2 * q + 1] = make_float2(v1.z, v1.w);
+    }
+    S.prow_of[0] = (int)psw[i];
+    S.prow_of[1] = (int)psw[i + 16];
+    S.U = (uint64_t)psw[32] | ((uint64_t)psw[33] << 32);
+    S.mant = __uint_as_float(psw[34]);
+    S.expo = (int)psw[35];
+    S.neg = (int)(psw[36] & 1u);
+    S.ok = (psw[36] >> 1) & 1u;
+  }
+  S.half = half;
+  S.pbit[0] = 1ull << S.prow_of[0];
+  S.pbit[1] = 1ull << S.prow_of[1];
+  S.key = lu_pivot_key<64, 2, 0, 0, LU_PAIRED>(S, lane);
+  lu_phase<64, 2, 32, LU_PAIRED>(S, prow, lane);
+  lu_phase<64, 2, 16, LU_PAIRED>(S, prow, lane);
+  // each half's state -> both results
+  const float mo = __shfl_xor_sync(VMC_FULL_MASK, S.mant, 16);
+  const int eo = __shfl_xor_sync(VMC_FULL_MASK, S.expo, 16);
+  const int no = __shfl_xor_sync(VMC_FULL_MASK, S.neg, 16);
+  const bool oo = __shfl_xor_sync(VMC_FULL_MASK, (int)S.ok, 16) != 0;
+  const Det mine = lu_det(S.ok, S.mant, S.expo, S.neg), other = lu_det(oo, mo, eo, no);
+  d0 = half ? other : mine;
+  d1 = half ? mine : other;
+}
+
 // Two 64 x 64 matrices on one warp.  Each runs its first 32 pivot steps in
 // the full layout, then parks its 32 x 32 remainder in its own first 4 KB
 // (L2; the warp has consumed those rows) and its scalar state in the warp's
@@ -1080,13 +1144,90 @@ __device__ __forceinline__ bool ld_flag(const LdArgs& la, int64_t row) {
   return true;
 }
 
-// FP32 64 x 64 rows, two matrices a warp: a CTA of 4 warps takes 8 rows,
-// keeps those that need an evaluation and hands them out in pairs (warp w:
-// the (2w)-th and (2w+1)-th; at most one warp of a CTA is left with one).
-// Shared memory per warp: 128 floats of pivot-row slots + 2 x 40 words.
+// FP32 64 x 64 rows.  A CTA of 4 warps takes 4 rows and hands the ones that
+// need an evaluation to its warps in order; each warp runs its matrix's first
+// 32 pivot steps in the full layout (one matrix a warp, as many warps as
+// rows).  Warps 2k and 2k + 1 then meet at a named barrier: the odd warp parks
+// its 32 x 32 remainder in its own (consumed) orbital-matrix slot and its
+// scalar state in shared memory and retires; the even warp runs both tails as
+// one instruction stream (lu_tail_pair) and finishes both rows.  A warp
+// without a partner runs its tail alone in the same layout.
+// shared words per warp: 128 floats of pivot-row slots + parked state (k_logdet_dual: two 40-word blocks,
+// k_logdet_pair: one)
 constexpr int LDP_WARP_WORDS = 128 + 80;
+
+// Named barrier of warps 2k and 2k + 1 (ids 1 and 2; 0 is __syncthreads').
+__device__ __forceinline__ void pair_barrier(int warp) {
+  if (warp >> 1) asm volatile("bar.sync 2, 64;" ::: "memory");
+  else asm volatile("bar.sync 1, 64;" ::: "memory");
+}
 template <int MODE>
 __global__ void __launch_bounds__(128, LU_MIN_CTAS) k_logdet_pair(int64_t R, int64_t row0, float* A, LdArgs la) {
+  extern __shared__ __align__(16) uint8_t lsm[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t base = (int64_t)blockIdx.x * 4;
+  bool fl = false;
+  if (lane < 4 && base + lane < R) fl = ld_flag<MODE>(la, row0 + base + lane);
+  const unsigned mask = __ballot_sync(VMC_FULL_MASK, fl);
+  const int n = __popc(mask);
+  if (warp >= n) return;
+  // the warp's row: the warp-th set bit; its partner's: the (warp ^ 1)-th
+  unsigned m = mask;
+  for (int k = 0; k < warp; ++k) m &= m - 1u;
+  const int64_t l = base + (__ffs(m) - 1);
+  const bool paired = (warp ^ 1) < n;
+  if (MODE == LD_ACCEPT && la.n_eval && lane == 0) atomicAdd(la.n_eval, 1ull);
+  float* prow = reinterpret_cast<float*>(lsm) + warp * LDP_WARP_WORDS;
+  float* Am = A + (size_t)l * 4096;
+  LuRegs<64> S;
+  lu_load<64>(S, Am, lane);
+  lu_phase<64, 2, 64, LU_FULL>(S, prow, lane);
+  lu_phase<64, 2, 48, LU_FULL>(S, prow, lane);
+  const int orow = lu_compact<32>(S, lane);
+  if (paired && (warp & 1)) {
+    __syncwarp();  // every lane's loads of the matrix precede the parking stores
+    float4* park = reinterpret_cast<float4*>(Am);
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+      __stcg(park + q * 32 + lane,
+             make_float4(S.a[0][2 * q].x, S.a[0][2 * q].y, S.a[0][2 * q + 1].x, S.a[0][2 * q + 1].y));
+    uint32_t* w = reinterpret_cast<uint32_t*>(prow + 128);
+    w[lane] = (uint32_t)orow;
+    if (lane == 0) {
+      w[32] = (uint32_t)S.U;
+      w[33] = (uint32_t)(S.U >> 32);
+      w[34] = __float_as_uint(S.mant);
+      w[35] = (uint32_t)S.expo;
+      w[36] = (uint32_t)S.neg | ((uint32_t)S.ok << 1);
+    }
+    pair_barrier(warp);
+    return;   // the even partner finishes this row
+  }
+  Det d0, d1;
+  int64_t lp = l;
+  if (paired) {
+    pair_barrier(warp);
+    m &= m - 1u;
+    lp = base + (__ffs(m) - 1);
+    const float* pw = reinterpret_cast<const float*>(lsm) + (warp + 1) * LDP_WARP_WORDS;
+    lu_tail_pair(S, orow, reinterpret_cast<const float4*>(A + (size_t)lp * 4096),
+                 reinterpret_cast<const uint32_t*>(pw + 128), prow, d0, d1);
+  } else {
+    lu_tail_pair(S, orow, nullptr, nullptr, prow, d0, d1);
+  }
+  const int nd = paired ? 2 : 1;
+#pragma unroll 1
+  for (int k = 0; k < nd; ++k) ld_finish<float, MODE>(row0 + (k ? lp : l), k ? d1 : d0, la, lane);
+}
+
+// FP32 64 x 64 rows, two matrices a warp throughout: a CTA of 4 warps takes
+// 8 rows and hands the ones that need an evaluation out in pairs (warp w: the
+// (2w)-th and (2w+1)-th; at most one warp of a CTA is left with one), see
+// warp_logdet_f32_pair.  Half as many warps as k_logdet_pair, each busy to
+// the end: the better choice when other launches (concurrent walker groups)
+// fill the SMs; alone on the GPU k_logdet_pair's warp per row wins.
+template <int MODE>
+__global__ void __launch_bounds__(128, LU_MIN_CTAS) k_logdet_dual(int64_t R, int64_t row0, float* A, LdArgs la) {
   extern __shared__ __align__(16) uint8_t lsm[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t base = (int64_t)blockIdx.x * 8;
@@ -1316,7 +1457,7 @@ int sweep_lanes() {
 
 int launch_eval_rows(int prec, int64_t R, int N, int nf, const uint64_t* row_occ, const void* net, double scale,
                      const Work& wk, int* err, cudaStream_t st, int ldmode, const LdArgs& la,
-                     bool allow_pipe = true) {
+                     bool allow_pipe = true, bool concurrent = false) {
   const int n_orb = 2 * N;
   if (prec == 0) {
     const NetF32& n = *(const NetF32*)net;
@@ -1367,13 +1508,20 @@ int launch_eval_rows(int prec, int64_t R, int N, int nf, const uint64_t* row_occ
       }
       STAGE_BEGIN(3);
       const unsigned gl = (unsigned)((Rc + wpb - 1) / wpb);
-      if (nf == 64) {  // two rows a warp (the orbital-matrix slot is scratch: the LU parks in it)
-        const unsigned gp = (unsigned)((Rc + 2 * wpb - 1) / (2 * wpb));
+      if (nf == 64 && !concurrent) {  // warp pairs share the tails (the orbital-matrix slot is scratch: the LU parks in it)
+        const unsigned gp = (unsigned)((Rc + wpb - 1) / wpb);
         const size_t psmem = (size_t)wpb * LDP_WARP_WORDS * sizeof(float);
         if (ldmode == LD_ACCEPT) k_logdet_pair<LD_ACCEPT><<<gp, 32 * wpb, psmem, st>>>(Rc, c0, Ac, la);
         else if (ldmode == LD_EVAL) k_logdet_pair<LD_EVAL><<<gp, 32 * wpb, psmem, st>>>(Rc, c0, Ac, la);
         else if (ldmode == LD_ACCEPT_Q) k_logdet_pair<LD_ACCEPT_Q><<<gp, 32 * wpb, psmem, st>>>(Rc, c0, Ac, la);
         else k_logdet_pair<LD_ELOC><<<gp, 32 * wpb, psmem, st>>>(Rc, c0, Ac, la);
+      } else if (nf == 64) {  // two matrices a warp (concurrent walker groups fill the SMs)
+        const unsigned gp = (unsigned)((Rc + 2 * wpb - 1) / (2 * wpb));
+        const size_t psmem = (size_t)wpb * LDP_WARP_WORDS * sizeof(float);
+        if (ldmode == LD_ACCEPT) k_logdet_dual<LD_ACCEPT><<<gp, 32 * wpb, psmem, st>>>(Rc, c0, Ac, la);
+        else if (ldmode == LD_EVAL) k_logdet_dual<LD_EVAL><<<gp, 32 * wpb, psmem, st>>>(Rc, c0, Ac, la);
+        else if (ldmode == LD_ACCEPT_Q) k_logdet_dual<LD_ACCEPT_Q><<<gp, 32 * wpb, psmem, st>>>(Rc, c0, Ac, la);
+        else k_logdet_dual<LD_ELOC><<<gp, 32 * wpb, psmem, st>>>(Rc, c0, Ac, la);
       } else {
         if (ldmode == LD_ACCEPT) k_logdet<float, 32, LD_ACCEPT><<<gl, 32 * wpb, lsmem, st>>>(Rc, c0, nf, Ac, la);
         else if (ldmode == LD_EVAL) k_logdet<float, 32, LD_EVAL><<<gl, 32 * wpb, lsmem, st>>>(Rc, c0, nf, Ac, la);
@@ -1541,7 +1689,7 @@ int vmc_nnbf_sweep(int prec, const void* const* net_ptrs, int n_sites, int nf, i
                                                    sweep_offset + (uint64_t)s, r_move, r_bit, r_acc,
                                                    (const float*)z0, nf32.w0t, prop_occ, (PropRec*)rec, H1);
           int rc = launch_eval_rows(prec, w1 - w0, n_sites, nf, prop_occ + 2 * w0, net, bf_scale, wg, d_err, gs,
-                                    LD_ACCEPT, lg, /*allow_pipe=*/false);
+                                    LD_ACCEPT, lg, /*allow_pipe=*/false, /*concurrent=*/true);
           if (rc) { g_timer.acc = nullptr; return rc; }
         }
       }
@@ -1659,7 +1807,7 @@ int vmc_nnbf_local_energy(int prec, const void* const* net_ptrs, int n_sites, in
       la.sign = const_cast<double*>(sign);
       la.logabs = const_cast<double*>(logabs);
       int rc = launch_eval_rows(prec, R, n_sites, nf, ro, net, bf_scale, wg, d_err, gs, LD_ELOC, la,
-                                /*allow_pipe=*/false);
+                                /*allow_pipe=*/false, /*concurrent=*/true);
       if (rc) return rc;
     }
     for (int g = 0; g < G; ++g)
