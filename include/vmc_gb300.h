@@ -102,6 +102,8 @@ int vmc_slater_logpsi_grad(const double* G, const uint8_t* slot_orb, int64_t B, 
  *   [3] b1 (256) f32/f64          [4] out_w (2N*nf, 256) bf16/f64
  *   [5] out_b (2N*nf) f32/f64     [6] M_base (2N, nf) f32/f64
  * Workspace for R rows (caller-owned): H1, H2 (R, 256) bf16/f64; A (R, nf, nf) f32/f64.
+ * The workspace is scratch: its contents on return are unspecified (the LU
+ * reuses consumed orbital-matrix rows).
  * d_err (device int) receives VMC_ERR_TIMEOUT if a bounded device wait gave up. */
 /* Evaluate R configurations from scratch: sign/logabs (R), and z0 = W0 n + b0
  * (R, 256) f32/f64 when z0_out is non-null.  Replaces forward_log / vamp_log
