@@ -418,9 +418,8 @@ def run_gb300(args):
     dom = int(np.argmax(stage_ms))
     kern_flops = [0.0, l1_flops, bf_flops, lu_flops]
     achieved = kern_flops[dom] / (stage_ms[dom] / 1e3) / 1e12
-    # DRAM bytes per LU launch (4096-row chunk) from one ncu capture of the kernel the
-    # per-kernel pass times (profiles/k_logdet_pair_8x8_chunk4096.md: dram read 52.57 MB +
-    # write 0.07 MB, cold cache)
+    # DRAM bytes per LU launch (4096-row chunk) from one ncu capture (cold cache) of the
+    # kernel the per-kernel pass times: dram read 52.57 MB + write 0.07 MB
     lu_traffic = 52.568832e6 + 0.067328e6 if dom == 3 else None
     roofline = {"bound": "tensor", "achieved": achieved, "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
                 "frac": achieved / pk["bf16_tflops"], "traffic": lu_traffic,
