@@ -10,14 +10,16 @@ from .hamiltonian import SpinfulFermion, SquareLattice, spinful_Fermi_Hubbard_sq
 from .models import FPEPS_GB300, NNBF_GB300, SlaterDeterminant_GB300, WavefunctionModel_GB300
 from .optimizer import FactoredO, MinSRGB300, SGDGB300
 from .sampler import MetropolisExchangeSpinfulSamplerGB300
-from .symmetry import FermionSymmetryProjectedModel_GB300
+from .symmetry import FermionSymmetryProjectedModel_GB300, build_symmetry_group
 from .vmc import VMC_GB300, VMCLoopConfig
 from .walkers import init_walkers, pack, unpack
 
 __all__ = [
-    "SquareLattice", "SpinfulFermion", "FPEPS_GB300", "FermionSymmetryProjectedModel_GB300", "spinful_Fermi_Hubbard_square_lattice_torch", "SlaterDeterminant_GB300", "NNBF_GB300",
-    "WavefunctionModel_GB300", "MetropolisExchangeSpinfulSamplerGB300", "evaluate_energy", "compute_grads_gpu",
-    "MinSRGB300", "SGDGB300", "FactoredO", "compute_grads_factored", "VMC_GB300", "VMCLoopConfig", "pack", "unpack", "init_walkers",
+    "SquareLattice", "SpinfulFermion", "spinful_Fermi_Hubbard_square_lattice_torch",
+    "WavefunctionModel_GB300", "SlaterDeterminant_GB300", "NNBF_GB300", "FPEPS_GB300",
+    "FermionSymmetryProjectedModel_GB300", "build_symmetry_group",
+    "MetropolisExchangeSpinfulSamplerGB300", "evaluate_energy", "compute_grads_gpu", "compute_grads_factored",
+    "MinSRGB300", "SGDGB300", "FactoredO", "VMC_GB300", "VMCLoopConfig", "pack", "unpack", "init_walkers",
 ]
 
 
