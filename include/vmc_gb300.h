@@ -3,8 +3,9 @@
  *
  * Every entry point takes raw device pointers, sizes and a cudaStream_t (passed
  * as void*), enqueues work on that stream and returns a status code; it never
- * allocates, frees or synchronises caller memory.  Host wrappers turn status
- * codes into the reference's exceptions.
+ * allocates or frees caller memory.  Two calls synchronise the stream and say
+ * so below: vmc_nnbf_sweep with stage timing, and vmc_check_finite with host
+ * counts.  Host wrappers turn status codes into the reference's exceptions.
  *
  * Walker layout: occ[2*w] = up bits, occ[2*w+1] = down bits (site i -> bit i,
  * n_sites <= 64).  Configurations at the API boundary use the reference's
@@ -25,6 +26,7 @@
  *   vmc_slater_local_energy      — _evaluate_energy_impl, vmc_torch/GPU/vmc_utils.py:322-476
  *   vmc_slater_logpsi_grad       — compute_grads_gpu, vmc_torch/GPU/vmc_utils.py:1389-1634
  *   vmc_sr_*                     — minSR_solver_gpu, vmc_torch/GPU/optimizer.py:471-614
+ *   vmc_check_finite             — _check_grads_amps, vmc_torch/GPU/vmc_utils.py:1330-1386
  *   vmc_energy_gradient          — the run_sr=False branch, vmc_torch/GPU/optimizer.py:585-613
  *   vmc_peps_eval / _sweep /     — fPEPS_Model_GPU.amplitude / log_amplitude,
  *   _local_energy                  vmc_torch/GPU/models/pureTNS.py:82-146, driven by
@@ -104,7 +106,14 @@ int vmc_slater_logpsi_grad(const double* G, const uint8_t* slot_orb, int64_t B, 
  * Workspace for R rows (caller-owned): H1, H2 (R, 256) bf16/f64; A (R, nf, nf) f32/f64.
  * The workspace is scratch: its contents on return are unspecified (the LU
  * reuses consumed orbital-matrix rows).
- * d_err (device int) receives VMC_ERR_TIMEOUT if a bounded device wait gave up. */
+ * d_err (device int) receives VMC_ERR_TIMEOUT if a bounded device wait gave up,
+ * and VMC_ERR_ARGS if a configuration evaluated from scratch has an occupation
+ * bit at or above n_sites or other than nf electrons (its result is then
+ * meaningless; bits above n_sites are ignored, never used as indices).
+ * Amplitude results: a singular orbital matrix gives sign 0 and logabs -inf; a
+ * NaN or Inf entry (non-finite parameters) gives NaN for both, as the
+ * reference's NaN amplitude.  Metropolis tests never accept a NaN ratio; from a
+ * zero-amplitude walker every non-zero proposal is accepted. */
 /* Evaluate R configurations from scratch: sign/logabs (R), and z0 = W0 n + b0
  * (R, 256) f32/f64 when z0_out is non-null.  Replaces forward_log / vamp_log
  * (vmc_torch/GPU/models/_base.py:101-130). */
@@ -196,6 +205,17 @@ int vmc_prop_inputs_f32(int n_sites, const uint64_t* occ, int64_t R, float* Xf, 
 int vmc_prop_collect_targets(const int32_t* pairs, int64_t P, const double* term, double t_abs, int n_hops,
                              int64_t row0, float* tgt, void* stream);
 
+/* Second network layer on the tensor cores: H2 = gelu(H1 W1^T + b1), H1 (R, 256)
+ * and W1 (256, 256) BF16, b1 (256) FP32, H2 (R, 256) BF16 (the stage the NNBF
+ * entry points run internally; no reference counterpart as an operator of its
+ * own, it is the second layer of NNBF_GPU, vmc_torch/GPU/models/NNBF.py:113-162).
+ * wait_limit_ns bounds the kernel's wait for its operand tiles (0: 1 s).
+ * skip_loads = 1 issues no tile load, so that the wait runs out with nothing in
+ * flight: d_err then receives VMC_ERR_TIMEOUT, H2 is left untouched and the
+ * context stays usable (the self-test of the bounded-wait path). */
+int vmc_nnbf_hidden_layer(const void* H1, int64_t R, const void* W1, const float* b1, void* H2,
+                          uint64_t wait_limit_ns, int skip_loads, int* d_err, void* stream);
+
 /* Allocation-free variant of vmc_nnbf_eval (mixed precision only, no z0 output).
  * This entry point has no counterpart in the reference.  It is for callers that
  * cannot allocate device memory while they run (a fixed device-memory budget
@@ -203,13 +223,31 @@ int vmc_prop_collect_targets(const int32_t* pairs, int64_t P, const double* term
  * pool): it takes no workspace and allocates nothing; its scratch is a fixed
  * 8.5 MiB array inside the library, held by every GPU that loads the library
  * until the process exits.  At most 512 configurations per call (nf <= 64);
- * larger R returns VMC_ERR_CAPACITY.  The first call on each device resolves the
- * array's device address (cudaGetSymbolAddress) and should come before any
- * stream capture.  All calls share the one array: calls whose work overlaps on
+ * larger R returns VMC_ERR_CAPACITY.  With CUDA's lazy module loading (the
+ * default) the array is committed on a device only when the library's module is
+ * first loaded there: the first call on each device does that, resolves the
+ * array's device address (cudaGetSymbolAddress) and sets the kernels'
+ * shared-memory attributes.  A caller that may not allocate later makes one
+ * warm-up call on each device first, before any no-allocation region and
+ * before any stream capture.  All calls share the one array: calls whose work overlaps on
  * the GPU (different streams, or different host threads) race on it and must
  * be serialised by the caller. */
 int vmc_nnbf_eval_noalloc(const void* const* net_ptrs, int n_sites, int nf, int hidden, double bf_scale,
                           const uint64_t* occ, int64_t R, double* sign, double* logabs, int* d_err, void* stream);
+
+/* ---- non-finite and zero-amplitude detection (_check_grads_amps,
+ * vmc_torch/GPU/vmc_utils.py:1330-1386) ----
+ * Counts into d_counts (4 device u64, cleared by the call): [0] NaN and [1] Inf
+ * entries of amp (B, nullable), [2] zero entries of sign (B, nullable), [3] rows
+ * of O (B, Np, leading dim ldo, dtype 0 f64 / 1 f32, nullable) holding a NaN or
+ * Inf.  d_row_bad (B) / d_col_bad (Np) flag those rows and columns (nullable).
+ * With h_counts (host, 4) non-null the call copies the counts there,
+ * synchronises the stream and returns VMC_ERR_NONFINITE if anything is NaN or
+ * Inf, else VMC_ERR_SINGULAR if some amplitude is zero, else VMC_OK; with
+ * h_counts null it only enqueues the work and returns VMC_OK. */
+int vmc_check_finite(const double* amp, const double* sign, int64_t B, const void* O, int dtype, int64_t Np,
+                     int64_t ldo, unsigned long long* d_counts, uint8_t* d_row_bad, uint8_t* d_col_bad,
+                     unsigned long long* h_counts, void* stream);
 
 /* ---- minSR in sample space (dtype: 0 = float64, 1 = float32 for O / Oc) ---- */
 int vmc_sr_center(const void* O, int dtype, int64_t Ns, int64_t Np, int64_t ldo, void* Oc, int64_t ldc, double* mean,

@@ -16,14 +16,24 @@ import numpy as np
 
 
 def minsr(O, E, energy_mean, diag_shift):
+    return minsr_with_info(O, E, energy_mean, diag_shift)[0]
+
+
+def minsr_with_info(O, E, energy_mean, diag_shift):
+    """(dp, info): LU solve of T x = E~, and when T is exactly singular the
+    least-squares fallback with info = 1 (vmc_torch/GPU/optimizer.py:557-561;
+    numpy's lstsq gives the minimum-norm solution)."""
     O = np.asarray(O, np.float64)
     E = np.asarray(E, np.float64)
     Ns = O.shape[0]
     Oc = (O - O.mean(axis=0, keepdims=True)) / np.sqrt(Ns)
     Es = (E - energy_mean) / np.sqrt(Ns)
     T = Oc @ Oc.T + diag_shift * np.eye(Ns)
-    x = np.linalg.solve(T, Es)
-    return Oc.T @ x
+    try:
+        x, info = np.linalg.solve(T, Es), 0
+    except np.linalg.LinAlgError:
+        x, info = np.linalg.lstsq(T, Es, rcond=None)[0], 1
+    return Oc.T @ x, info
 
 
 def energy_gradient(O, E, energy_mean):

@@ -63,3 +63,31 @@ def test_noalloc_rejects_batches_beyond_capacity():
     X = torch.as_tensor(lattice.random_initial_configs(CAPACITY + 1, 64, 32, 32, seed=5), device=DEV)
     st, _, _, _ = _noalloc(m, vg.pack(X), CAPACITY + 1)
     assert st == _lib.VMC_ERR_CAPACITY
+
+
+def test_noalloc_allocates_nothing_after_its_first_call():
+    """After one warm-up call (which loads the library's module on the device,
+    committing the fixed array, and resolves its address), a full-capacity call
+    takes no device memory: the free memory the driver reports (which counts
+    allocations made outside torch as well) does not drop, and torch's own
+    allocator holds exactly the caller's tensors."""
+    m = _model()
+    X = torch.as_tensor(lattice.random_initial_configs(CAPACITY, 64, 32, 32, seed=6), device=DEV)
+    occ = vg.pack(X)
+    st, _, _, _ = _noalloc(m, occ, CAPACITY)   # warm-up
+    assert st == 0
+    ts, arr = m.net(occ.device)
+    sign = torch.empty(CAPACITY, dtype=torch.float64, device=DEV)
+    logabs = torch.empty_like(sign)
+    err = torch.zeros(1, dtype=torch.int32, device=DEV)
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    held0 = torch.cuda.memory_allocated()
+    st = _lib.load().vmc_nnbf_eval_noalloc(arr, 64, 64, 256, m.bf_scale, _lib.ptr(occ), CAPACITY, _lib.ptr(sign),
+                                           _lib.ptr(logabs), _lib.ptr(err), _lib.stream_of(occ.device))
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert st == 0 and int(err.item()) == 0
+    assert torch.cuda.memory_allocated() == held0
+    assert free1 >= free0 - (1 << 20), "the call took %d bytes of device memory" % (free0 - free1)
+

@@ -46,6 +46,8 @@ SIGNATURES = {
     "vmc_nnbf_sweep": [I32, P, I32, I32, I32, F64, P, I64, P, I32, I32, F32, U64, U64, P, P, P, P, P, P, P, P, P,
                        P, P, P, P, P, P, P, P],
     "vmc_nnbf_eval_noalloc": [P, I32, I32, I32, F64, P, I64, P, P, P, P],
+    "vmc_nnbf_hidden_layer": [P, I64, P, P, P, U64, I32, P, P],
+    "vmc_check_finite": [P, P, I64, P, I32, I64, I64, P, P, P, P, P],
     "vmc_prop_logits": [P, I32, P, I64, P, P, P, P, P, P],
     "vmc_prop_sample": [P, I32, I32, P, P, I64, U64, U64, P, P, P],
     "vmc_prop_reverse": [P, I32, I32, P, P, I64, P, P],
@@ -120,6 +122,20 @@ def call(name, *args):
     if st != VMC_OK:
         raise ValueError("%s failed: %s (status %d)" % (name, _MSG.get(st, "unknown"), st))
     return st
+
+
+def call_status(name, *args, allow=()):
+    """Call an entry point; return its status when it is VMC_OK or in
+    ``allow`` (statuses that report a condition rather than a failure), else
+    raise."""
+    st = getattr(load(), name)(*args)
+    if st != VMC_OK and st not in allow:
+        raise ValueError("%s failed: %s (status %d)" % (name, _MSG.get(st, "unknown"), st))
+    return st
+
+
+def message(status):
+    return _MSG.get(status, "unknown status %d" % status)
 
 
 def require_cuda(t, what="tensor"):

@@ -133,13 +133,21 @@ __global__ void k_prep_sweep(int64_t B, int64_t w_begin, int64_t w_end, int N, c
 }
 
 // z0 = b0 + sum of W0 columns of the occupied orbitals (from scratch); h1 -> H1.
+// A configuration with an occupation bit at or above N, or with other than nf
+// electrons, sets *err = VMC_ERR_ARGS (its result is meaningless); the bits
+// above N are dropped here so that W0 is never indexed past its 2N rows.
 template <typename T>
-__global__ void k_prep_fresh(int64_t R, int N, const uint64_t* __restrict__ occ, const T* __restrict__ w0t,
-                             const T* __restrict__ b0, T* __restrict__ z0_out, void* __restrict__ H1) {
+__global__ void k_prep_fresh(int64_t R, int N, int nf, const uint64_t* __restrict__ occ, const T* __restrict__ w0t,
+                             const T* __restrict__ b0, T* __restrict__ z0_out, void* __restrict__ H1,
+                             int* __restrict__ err) {
   const int lane = threadIdx.x & 31;
   const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (w >= R) return;
-  const uint64_t up = occ[2 * w], dn = occ[2 * w + 1];
+  const uint64_t keep = bits_below(N);
+  const uint64_t up_raw = occ[2 * w], dn_raw = occ[2 * w + 1];
+  const uint64_t up = up_raw & keep, dn = dn_raw & keep;
+  if (lane == 0 && err && (((up_raw | dn_raw) & ~keep) != 0ull || __popcll(up) + __popcll(dn) != nf))
+    atomicExch(err, VMC_ERR_ARGS);
   T h[8];
 #pragma unroll
   for (int q = 0; q < 8; ++q) h[q] = b0[lane * 8 + q];
@@ -212,6 +220,11 @@ struct EpiArgs {
   float* Aout;                // (rows, nf, nf)
   float scale;
   int n_sites, nf;
+  // bounded wait for the operand tiles (0: 1 s); skip_loads issues no tile
+  // load, so that the wait runs out with nothing in flight (self-test of the
+  // timeout path, vmc_nnbf_hidden_layer)
+  uint64_t wait_ns;
+  int skip_loads;
 };
 
 template <int EPI>
@@ -252,12 +265,14 @@ __global__ void __launch_bounds__(128, 1)
   tc::fence_after_sync();
   const uint32_t tbase = *tslot;
   if (threadIdx.x == 0) {
-    tc::mbar_arrive_expect_tx(&bars[0], SMEM_A + SMEM_B);
+    if (!ea.skip_loads) {
+      tc::mbar_arrive_expect_tx(&bars[0], SMEM_A + SMEM_B);
 #pragma unroll
-    for (int j = 0; j < 4; ++j) tc::tma_load_2d(sA + j * (TM * 128), &tmA, &bars[0], j * 64, row0);
+      for (int j = 0; j < 4; ++j) tc::tma_load_2d(sA + j * (TM * 128), &tmA, &bars[0], j * 64, row0);
 #pragma unroll
-    for (int j = 0; j < 4; ++j) tc::tma_load_2d(sB + j * (TN * 128), &tmB, &bars[0], j * 64, brow0);
-    if (tc::mbar_wait(&bars[0], 0)) {
+      for (int j = 0; j < 4; ++j) tc::tma_load_2d(sB + j * (TN * 128), &tmB, &bars[0], j * 64, brow0);
+    }
+    if (tc::mbar_wait(&bars[0], 0, ea.wait_ns ? ea.wait_ns : 1000000000ull)) {
       tc::fence_after_sync();
       constexpr uint32_t idesc = tc::idesc_bf16_f32(TM, TN);
 #pragma unroll
@@ -579,7 +594,7 @@ struct LuRegs {
   float2 a[NF / 32][NF / 2];
   uint64_t U;
   float mant;
-  int expo, neg;
+  int expo, neg;   // neg bit 0: sign of the determinant; bit 1: a non-finite pivot was met
   bool ok;
   unsigned key;   // pivot key of the next step (computed one step ahead)
   // paired layout: original rows of the two register rows, their bits, and
@@ -631,7 +646,9 @@ template <int NF>
 __device__ __forceinline__ float lu_pivot_update(LuRegs<NF>& S, unsigned key, int p, float pv) {
   const float best = __uint_as_float(key & ~63u);
   const bool pvalid = key != 0u && (best > 0.0f) && isfinite(best);
-  if (!pvalid) { S.ok = false; pv = 1.0f; }
+  // NaN and Inf keys order above every finite one, so a non-finite entry of
+  // the pivot column is always the candidate that is seen here
+  if (!pvalid) { S.ok = false; S.neg |= (key != 0u && !isfinite(best)) ? 2 : 0; pv = 1.0f; }
   S.neg ^= (pv < 0.0f);
   S.neg ^= __popcll(S.U & ((1ull << p) - 1ull)) & 1;
   S.U &= ~(1ull << p);
@@ -793,9 +810,15 @@ __device__ __forceinline__ void lu_load(LuRegs<NF>& S, const float* __restrict__
   S.key = lu_pivot_key<NF, R, 0, 0, LU_FULL>(S, lane);
 }
 
+// Singular matrices give sign 0 and log|det| = -inf; a non-finite entry
+// (NaN or Inf parameters upstream) gives NaN for both, like the reference's
+// NaN amplitude.
 __device__ __forceinline__ Det lu_det(bool ok, float mant, int expo, int neg) {
   Det d;
-  if (ok) {
+  if (!ok && (neg & 2)) {
+    d.logabs = __longlong_as_double(0x7ff8000000000000ll);
+    d.sign = d.logabs;
+  } else if (ok) {
     // mantissa in [1, 2): FP32 log is accurate to ~1e-7 absolute; the exponent
     // part is exact; only the final sum is FP64 (FP64 pipes are scarce on GB300)
     d.logabs = (double)logf(mant) + (double)expo * 0.69314718055994530942;
@@ -819,6 +842,13 @@ __device__ __forceinline__ Det warp_logdet_f32(const float* __restrict__ A, floa
   lu_phase<NF, 1, NF - 16, LU_FULL>(S, prow, lane);
   return lu_det(S.ok, S.mant, S.expo, S.neg);
 }
+
+// Scalar LU state word of a parked remainder: bit 0 determinant sign, bit 1
+// ok, bit 2 non-finite pivot met.
+__device__ __forceinline__ uint32_t park_flags(int neg, bool ok) {
+  return (uint32_t)(neg & 1) | ((uint32_t)ok << 1) | ((uint32_t)(neg & 2) << 1);
+}
+__device__ __forceinline__ int unpark_neg(uint32_t w) { return (int)((w & 1u) | ((w >> 1) & 2u)); }
 
 // Last 32 pivot steps of a 64 x 64 matrix whose first 32 ran on this warp
 // (S after lu_compact, lane L holding live row L, orow its original row),
@@ -865,7 +895,7 @@ __device__ __forceinline__ void lu_tail_pair(LuRegs<64>& S, int orow, const floa
     S.U = (uint64_t)psw[32] | ((uint64_t)psw[33] << 32);
     S.mant = __uint_as_float(psw[34]);
     S.expo = (int)psw[35];
-    S.neg = (int)(psw[36] & 1u);
+    S.neg = unpark_neg(psw[36]);
     S.ok = (psw[36] >> 1) & 1u;
   }
   S.half = half;
@@ -919,7 +949,7 @@ __device__ __forceinline__ void warp_logdet_f32_pair(float* A, float* prow, uint
       w[33] = (uint32_t)(S.U >> 32);
       w[34] = __float_as_uint(S.mant);
       w[35] = (uint32_t)S.expo;
-      w[36] = (uint32_t)S.neg | ((uint32_t)S.ok << 1);
+      w[36] = park_flags(S.neg, S.ok);
     }
   }
   __syncwarp();  // parked rows and words visible to every lane
@@ -941,7 +971,7 @@ __device__ __forceinline__ void warp_logdet_f32_pair(float* A, float* prow, uint
   S.U = (uint64_t)w[32] | ((uint64_t)w[33] << 32);
   S.mant = __uint_as_float(w[34]);
   S.expo = (int)w[35];
-  S.neg = (int)(w[36] & 1u);
+  S.neg = unpark_neg(w[36]);
   S.ok = (w[36] >> 1) & 1u;
   S.half = half;
   S.pbit[0] = 1ull << S.prow_of[0];
@@ -968,13 +998,14 @@ __device__ Det warp_logdet_f64(const double* __restrict__ A, int nf, double* s /
   uint64_t U = (nf == 64) ? ~0ull : ((1ull << nf) - 1ull);
   double la = 0.0;
   int neg = 0;
-  bool ok = true;
+  bool ok = true, nonfinite = false;
   for (int k = 0; k < nf; ++k) {
     double best = -1.0;
     int bi = 1 << 30;
     for (int r = lane; r < nf; r += 32) {
       if ((U >> r) & 1ull) {
-        const double v = fabs(s[r * ld + k]);
+        double v = fabs(s[r * ld + k]);
+        if (v != v) v = INFINITY;   // NaN ranks first, so that it is detected
         if (v > best) { best = v; bi = r; }
       }
     }
@@ -987,7 +1018,11 @@ __device__ Det warp_logdet_f64(const double* __restrict__ A, int nf, double* s /
     const int p = bi;
     if (p >= nf) { ok = false; break; }  // no finite pivot candidate (warp-uniform)
     double pv = s[p * ld + k];
-    if (!(best > 0.0) || !isfinite(best)) { ok = false; pv = 1.0; }
+    if (!(best > 0.0) || !isfinite(best)) {
+      nonfinite |= !isfinite(best);
+      ok = false;
+      pv = 1.0;
+    }
     neg ^= (pv < 0.0);
     neg ^= __popcll(U & ((1ull << p) - 1ull)) & 1;
     U &= ~(1ull << p);
@@ -1002,8 +1037,13 @@ __device__ Det warp_logdet_f64(const double* __restrict__ A, int nf, double* s /
     __syncwarp();
   }
   Det d;
-  d.logabs = ok ? la : -INFINITY;
-  d.sign = ok ? (neg ? -1.0 : 1.0) : 0.0;
+  if (nonfinite) {
+    d.logabs = __longlong_as_double(0x7ff8000000000000ll);
+    d.sign = d.logabs;
+  } else {
+    d.logabs = ok ? la : -INFINITY;
+    d.sign = ok ? (neg ? -1.0 : 1.0) : 0.0;
+  }
   return d;
 }
 
@@ -1058,10 +1098,13 @@ __device__ __forceinline__ void ld_finish(int64_t row, const Det& d, const LdArg
     }
   } else if (MODE == LD_ACCEPT_Q) {
     const PropRec4 r = la.rec4[row];
-    // Metropolis-Hastings with the proposal ratio q(x'->x)/q(x->x')
-    const float la2 = (float)(2.0 * (d.logabs - la.logabs[row])) + (r.logq_rev - r.logq_fwd);
+    // Metropolis-Hastings with the proposal ratio q(x'->x)/q(x->x').  Every
+    // lane reads the current log-amplitude before lane 0 may overwrite it.
+    const double cur = __shfl_sync(VMC_FULL_MASK, lane == 0 ? la.logabs[row] : 0.0, 0);
+    const float la2 = (float)(2.0 * (d.logabs - cur)) + (r.logq_rev - r.logq_fwd);
     const float prob = expf(fminf(la2, 80.0f));
-    const bool acc = (d.sign != 0.0) && isfinite(r.logq_rev) && (r.u_acc < prob);
+    // a NaN ratio (NaN amplitude on either side) never accepts, as u < NaN is false
+    const bool acc = (d.sign != 0.0) && (la2 == la2) && isfinite(r.logq_rev) && (r.u_acc < prob);
     const int kk = min(max(r.k, 1), 4) - 1;
     if (la.kstats && lane == 0) {
       atomicAdd(&la.kstats[kk], 1);
@@ -1086,10 +1129,14 @@ __device__ __forceinline__ void ld_finish(int64_t row, const Det& d, const LdArg
   } else {
     const PropRec r = la.rec[row];
     // |psi'|^2/|psi|^2 from the FP64 log difference, exponentiated in FP32
-    // (FP32 relative accuracy is ample for comparing against a 24-bit uniform)
-    const float dl2 = (float)(2.0 * (d.logabs - la.logabs[row]));
+    // (FP32 relative accuracy is ample for comparing against a 24-bit uniform).
+    // Every lane reads the current log-amplitude before lane 0 may overwrite it.
+    const double cur = __shfl_sync(VMC_FULL_MASK, lane == 0 ? la.logabs[row] : 0.0, 0);
+    const float dl2 = (float)(2.0 * (d.logabs - cur));
     const float prob = expf(fminf(dl2, 80.0f));
-    const bool acc = (d.sign != 0.0) && (r.u_acc < prob);
+    // a NaN ratio (NaN amplitude on either side) never accepts, as u < NaN is false;
+    // from a zero-amplitude walker (cur = -inf) every non-zero proposal accepts
+    const bool acc = (d.sign != 0.0) && (dl2 == dl2) && (r.u_acc < prob);
     if (!acc) return;
     if (lane == 0) {
       la.occ[2 * row] = la.prop_occ[2 * row];
@@ -1198,7 +1245,7 @@ __global__ void __launch_bounds__(128, LU_MIN_CTAS) k_logdet_pair(int64_t R, int
       w[33] = (uint32_t)(S.U >> 32);
       w[34] = __float_as_uint(S.mant);
       w[35] = (uint32_t)S.expo;
-      w[36] = (uint32_t)S.neg | ((uint32_t)S.ok << 1);
+      w[36] = park_flags(S.neg, S.ok);
     }
     pair_barrier(warp);
     return;   // the even partner finishes this row
@@ -1484,13 +1531,22 @@ int launch_eval_rows(int prec, int64_t R, int N, int nf, const uint64_t* row_occ
       if (cudaEventRecord(pipe->h2, st) != cudaSuccess || cudaStreamWaitEvent(pipe->aux, pipe->h2, 0) != cudaSuccess)
         return VMC_ERR_CUDA;
     }
+    // on an error after the first chunk the caller's stream waits for what is
+    // already queued on the second stream before the error is returned
+    auto fail = [&](int rc) {
+      if (pipe) {
+        cudaEventRecord(pipe->h2, pipe->aux);
+        cudaStreamWaitEvent(st, pipe->h2, 0);
+      }
+      return rc;
+    };
     for (int64_t ci = 0; ci < n_chunks; ++ci) {
       const int64_t c0 = ci * CH;
       const int64_t Rc = (R - c0) < CH ? (R - c0) : CH;
       const int slot = pipe ? (int)(ci & 1) : 0;
       float* Ac = (float*)wk.A + (size_t)slot * (size_t)CH * nf * nf;
       CUtensorMap tH2c;
-      if (!tmap_bf16(&tH2c, (const __nv_bfloat16*)wk.H2 + c0 * HID, (uint64_t)Rc, TM)) return VMC_ERR_UNSUPPORTED;
+      if (!tmap_bf16(&tH2c, (const __nv_bfloat16*)wk.H2 + c0 * HID, (uint64_t)Rc, TM)) return fail(VMC_ERR_UNSUPPORTED);
       PBArgs pa{};
       pa.row_occ = row_occ + 2 * c0; pa.mbase = n.mbase; pa.outb = n.outb; pa.Aout = Ac;
       pa.scale = (float)scale; pa.n_sites = N; pa.nf = nf; pa.R = (int)Rc;
@@ -1498,13 +1554,13 @@ int launch_eval_rows(int prec, int64_t R, int N, int nf, const uint64_t* row_occ
       pa.n_items = n_groups * pa.n_tiles;
       const int grid = pa.n_items < num_sms() ? pa.n_items : num_sms();
       cudaStream_t gs = pipe ? pipe->aux : st;
-      if (pipe && ci >= 2 && cudaStreamWaitEvent(gs, pipe->lu[slot], 0) != cudaSuccess) return VMC_ERR_CUDA;
+      if (pipe && ci >= 2 && cudaStreamWaitEvent(gs, pipe->lu[slot], 0) != cudaSuccess) return fail(VMC_ERR_CUDA);
       STAGE_BEGIN(2);
       k_backflow_persistent<<<grid, PB_THREADS, PB_SMEM, gs>>>(tH2c, tOW, pa, err);
       STAGE_END(2);
       if (pipe) {
         if (cudaEventRecord(pipe->g[slot], gs) != cudaSuccess || cudaStreamWaitEvent(st, pipe->g[slot], 0) != cudaSuccess)
-          return VMC_ERR_CUDA;
+          return fail(VMC_ERR_CUDA);
       }
       STAGE_BEGIN(3);
       const unsigned gl = (unsigned)((Rc + wpb - 1) / wpb);
@@ -1529,7 +1585,7 @@ int launch_eval_rows(int prec, int64_t R, int N, int nf, const uint64_t* row_occ
         else k_logdet<float, 32, LD_ELOC><<<gl, 32 * wpb, lsmem, st>>>(Rc, c0, nf, Ac, la);
       }
       STAGE_END(3);
-      if (pipe && cudaEventRecord(pipe->lu[slot], st) != cudaSuccess) return VMC_ERR_CUDA;
+      if (pipe && cudaEventRecord(pipe->lu[slot], st) != cudaSuccess) return fail(VMC_ERR_CUDA);
     }
   } else {
     const NetF64& n = *(const NetF64*)net;
@@ -1591,13 +1647,13 @@ int vmc_nnbf_eval(int prec, const void* const* net_ptrs, int n_sites, int nf, in
     nf32 = NetF32{(const float*)net_ptrs[0], (const float*)net_ptrs[1], (const __nv_bfloat16*)net_ptrs[2],
                   (const float*)net_ptrs[3], (const __nv_bfloat16*)net_ptrs[4], (const float*)net_ptrs[5],
                   (const float*)net_ptrs[6]};
-    k_prep_fresh<float><<<gw, 256, 0, st>>>(R, n_sites, occ, nf32.w0t, nf32.b0, (float*)z0_out, H1);
+    k_prep_fresh<float><<<gw, 256, 0, st>>>(R, n_sites, nf, occ, nf32.w0t, nf32.b0, (float*)z0_out, H1, d_err);
     net = &nf32;
   } else {
     nf64 = NetF64{(const double*)net_ptrs[0], (const double*)net_ptrs[1], (const double*)net_ptrs[2],
                   (const double*)net_ptrs[3], (const double*)net_ptrs[4], (const double*)net_ptrs[5],
                   (const double*)net_ptrs[6]};
-    k_prep_fresh<double><<<gw, 256, 0, st>>>(R, n_sites, occ, nf64.w0t, nf64.b0, (double*)z0_out, H1);
+    k_prep_fresh<double><<<gw, 256, 0, st>>>(R, n_sites, nf, occ, nf64.w0t, nf64.b0, (double*)z0_out, H1, d_err);
     net = &nf64;
   }
   VMC_CUDA_CHECK_LAUNCH();
@@ -1690,7 +1746,14 @@ int vmc_nnbf_sweep(int prec, const void* const* net_ptrs, int n_sites, int nf, i
                                                    (const float*)z0, nf32.w0t, prop_occ, (PropRec*)rec, H1);
           int rc = launch_eval_rows(prec, w1 - w0, n_sites, nf, prop_occ + 2 * w0, net, bf_scale, wg, d_err, gs,
                                     LD_ACCEPT, lg, /*allow_pipe=*/false, /*concurrent=*/true);
-          if (rc) { g_timer.acc = nullptr; return rc; }
+          if (rc) {
+            // kernels already queued on this group's stream still write the
+            // caller's buffers: the caller's stream waits for them all the same
+            cudaEventRecord(pipe->join[g], gs);
+            cudaStreamWaitEvent(st, pipe->join[g], 0);
+            g_timer.acc = nullptr;
+            return rc;
+          }
         }
       }
       if (cudaEventRecord(pipe->join[g], gs) != cudaSuccess || cudaStreamWaitEvent(st, pipe->join[g], 0) != cudaSuccess)
@@ -1808,7 +1871,14 @@ int vmc_nnbf_local_energy(int prec, const void* const* net_ptrs, int n_sites, in
       la.logabs = const_cast<double*>(logabs);
       int rc = launch_eval_rows(prec, R, n_sites, nf, ro, net, bf_scale, wg, d_err, gs, LD_ELOC, la,
                                 /*allow_pipe=*/false, /*concurrent=*/true);
-      if (rc) return rc;
+      if (rc) {
+        // the caller's stream still waits for every kernel already queued on the lanes
+        for (int h = 0; h < G; ++h) {
+          cudaEventRecord(pipe->join[h], pipe->lane[h]);
+          cudaStreamWaitEvent(st, pipe->join[h], 0);
+        }
+        return rc;
+      }
     }
     for (int g = 0; g < G; ++g)
       if (cudaEventRecord(pipe->join[g], pipe->lane[g]) != cudaSuccess ||
@@ -1901,12 +1971,37 @@ extern "C" int vmc_nnbf_eval_noalloc(const void* const* net_ptrs, int n_sites, i
              (const float*)net_ptrs[3], (const __nv_bfloat16*)net_ptrs[4], (const float*)net_ptrs[5],
              (const float*)net_ptrs[6]};
   const unsigned gw = (unsigned)((R * 32 + 255) / 256);
-  k_prep_fresh<float><<<gw, 256, 0, st>>>(R, n_sites, occ, n32.w0t, n32.b0, nullptr, wk.H1);
+  k_prep_fresh<float><<<gw, 256, 0, st>>>(R, n_sites, nf, occ, n32.w0t, n32.b0, nullptr, wk.H1, d_err);
   VMC_CUDA_CHECK_LAUNCH();
   LdArgs la{};
   la.sign = sign;
   la.logabs = logabs;
   return launch_eval_rows(0, R, n_sites, nf, occ, &n32, bf_scale, wk, d_err, st, LD_EVAL, la);
+}
+
+// Second network layer on the tensor cores, H2 = gelu(H1 W1^T + b1) (BF16
+// operands, FP32 accumulation, BF16 result): the stage every mixed NNBF entry
+// point runs after the first layer.  It doubles as the self-test of the
+// bounded-wait path: with skip_loads = 1 the kernel issues no tile load, so
+// its wait for the operands runs out after wait_limit_ns with no copy or MMA
+// in flight; the kernel then records VMC_ERR_TIMEOUT in *d_err, frees its
+// tensor memory and returns, leaving H2 untouched and the context usable.
+extern "C" int vmc_nnbf_hidden_layer(const void* H1, int64_t R, const void* W1, const float* b1, void* H2,
+                                     uint64_t wait_limit_ns, int skip_loads, int* d_err, void* stream) {
+  if (R < 0 || R > (int64_t)INT32_MAX || (R > 0 && (!H1 || !W1 || !b1 || !H2 || !d_err))) return VMC_ERR_ARGS;
+  if (R == 0) return VMC_OK;
+  set_attrs();
+  CUtensorMap tH1, tW1;
+  if (!tmap_bf16(&tH1, H1, (uint64_t)R, TM) || !tmap_bf16(&tW1, W1, HID, TN)) return VMC_ERR_UNSUPPORTED;
+  EpiArgs e1{};
+  e1.bias = b1;
+  e1.out = (__nv_bfloat16*)H2;
+  e1.wait_ns = wait_limit_ns;
+  e1.skip_loads = skip_loads ? 1 : 0;
+  dim3 g1((unsigned)((R + TM - 1) / TM), 1);
+  k_gemm_tc<EPI_GELU_BF16><<<g1, 128, GEMM_SMEM, (cudaStream_t)stream>>>(tH1, tW1, (int)R, e1, d_err);
+  VMC_CUDA_CHECK_LAUNCH();
+  return VMC_OK;
 }
 
 // Metropolis-Hastings step with a learned proposal (mixed precision): the
@@ -1929,7 +2024,7 @@ extern "C" int vmc_nnbf_mh_step(const void* const* net_ptrs, int n_sites, int nf
              (const float*)net_ptrs[3], (const __nv_bfloat16*)net_ptrs[4], (const float*)net_ptrs[5],
              (const float*)net_ptrs[6]};
   const unsigned gw = (unsigned)((B * 32 + 255) / 256);
-  k_prep_fresh<float><<<gw, 256, 0, st>>>(B, n_sites, prop_occ, n32.w0t, n32.b0, (float*)z0p, H1);
+  k_prep_fresh<float><<<gw, 256, 0, st>>>(B, n_sites, nf, prop_occ, n32.w0t, n32.b0, (float*)z0p, H1, d_err);
   VMC_CUDA_CHECK_LAUNCH();
   LdArgs la{};
   la.rec4 = (const PropRec4*)rec4;

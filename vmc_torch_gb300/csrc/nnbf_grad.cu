@@ -113,12 +113,13 @@ __global__ void __launch_bounds__(256) k_nnbf_grad(GradNet<T> net, int N, int nf
   // ---- Gauss-Jordan inverse with partial pivoting ----
   double la = 0.0;
   int neg = 0;
-  for (int k = 0; k < nf && piv[1]; ++k) {
+  for (int k = 0; k < nf && piv[1] == 1; ++k) {
     if (tid < 32) {
       double best = -1.0;
       int bi = k;
       for (int r = k + tid; r < nf; r += 32) {
-        const double v = fabs((double)A[r * ldA + k]);
+        double v = fabs((double)A[r * ldA + k]);
+        if (v != v) v = INFINITY;   // NaN ranks first, so that it is detected
         if (v > best) { best = v; bi = r; }
       }
 #pragma unroll
@@ -129,11 +130,11 @@ __global__ void __launch_bounds__(256) k_nnbf_grad(GradNet<T> net, int N, int nf
       }
       if (tid == 0) {
         piv[0] = bi;
-        if (!(best > 0.0) || !isfinite(best)) piv[1] = 0;
+        if (!(best > 0.0) || !isfinite(best)) piv[1] = isfinite(best) ? 0 : -1;
       }
     }
     __syncthreads();
-    if (!piv[1]) break;
+    if (piv[1] != 1) break;
     const int p = piv[0];
     if (p != k) {
       for (int c = tid; c < 2 * nf; c += 256) {
@@ -164,10 +165,12 @@ __global__ void __launch_bounds__(256) k_nnbf_grad(GradNet<T> net, int N, int nf
     }
     __syncthreads();
   }
-  const bool ok = piv[1] != 0;
+  // piv[1]: 1 regular, 0 singular (or wrong electron count), -1 non-finite entry
+  const bool ok = piv[1] == 1;
   if (tid == 0) {
-    if (logabs_out) logabs_out[w] = ok ? la : -INFINITY;
-    if (sign_out) sign_out[w] = ok ? (neg ? -1.0 : 1.0) : 0.0;
+    const double qnan = __longlong_as_double(0x7ff8000000000000ll);
+    if (logabs_out) logabs_out[w] = ok ? la : (piv[1] < 0 ? qnan : -INFINITY);
+    if (sign_out) sign_out[w] = ok ? (neg ? -1.0 : 1.0) : (piv[1] < 0 ? qnan : 0.0);
   }
   // Gbar[orbs[pos]][c] = Ainv[c][pos]; stored as G[pos][c] in A (reuse)
   for (int idx = tid; idx < nf * nf; idx += 256) {

@@ -30,7 +30,9 @@ __device__ __forceinline__ int gstride(int nf) { return nf + 1; }
 
 // Full re-inversion by Gauss-Jordan with partial pivoting on [A | I] in
 // shared memory.  Resets slots to ascending occupied order.  aug: nf x (2nf+1),
-// fac: nf.  Writes G (stride nf+1) into g_out.  Returns false if singular.
+// fac: nf.  Writes G (stride nf+1) into g_out.  Returns false if singular or
+// non-finite; a non-finite entry (NaN/Inf parameters) gives NaN sign and
+// log-amplitude, a singular matrix sign 0 and -inf.
 __device__ bool warp_refresh(const double* __restrict__ M, int nf, int N, uint64_t up, uint64_t dn, double* aug,
                              double* fac, double* g_out, uint8_t* slot, double& sign, double& logabs) {
   const int lane = threadIdx.x & 31;
@@ -60,13 +62,14 @@ __device__ bool warp_refresh(const double* __restrict__ M, int nf, int N, uint64
   }
   __syncwarp();
   double s = 1.0, la = 0.0;
-  bool ok = true;
+  bool ok = true, nonfinite = false;
   for (int k = 0; k < nf; ++k) {
-    // pivot search over rows >= k (smallest index wins ties)
+    // pivot search over rows >= k (smallest index wins ties; NaN ranks first)
     double best = -1.0;
     int bi = k;
     for (int r = k + lane; r < nf; r += 32) {
       double v = fabs(aug[r * ld + k]);
+      if (v != v) v = INFINITY;
       if (v > best) { best = v; bi = r; }
     }
 #pragma unroll
@@ -75,7 +78,11 @@ __device__ bool warp_refresh(const double* __restrict__ M, int nf, int N, uint64
       int oi = __shfl_xor_sync(VMC_FULL_MASK, bi, o);
       if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
     }
-    if (!(best > 0.0) || !isfinite(best)) { ok = false; break; }
+    if (!(best > 0.0) || !isfinite(best)) {
+      nonfinite = !isfinite(best);
+      ok = false;
+      break;
+    }
     if (bi != k) {
       for (int c = lane; c < 2 * nf; c += 32) {
         double t0 = aug[k * ld + c];
@@ -105,8 +112,9 @@ __device__ bool warp_refresh(const double* __restrict__ M, int nf, int N, uint64
     g_out[k * gs + c] = ok ? aug[c * ld + nf + k] : 0.0;
   }
   __syncwarp();
-  sign = ok ? s : 0.0;
-  logabs = ok ? la : -INFINITY;
+  const double qnan = __longlong_as_double(0x7ff8000000000000ll);
+  sign = ok ? s : (nonfinite ? qnan : 0.0);
+  logabs = ok ? la : (nonfinite ? qnan : -INFINITY);
   return ok;
 }
 
@@ -150,7 +158,7 @@ __global__ void k_slater_refresh(const double* __restrict__ M, int nf, int N, co
     sign[w] = s;
     logabs[w] = la;
     if (n_acc) n_acc[w] = 0;
-    if (!ok && n_singular) atomicAdd(n_singular, 1);
+    if (!ok && s == 0.0 && n_singular) atomicAdd(n_singular, 1);   // singular, not non-finite
   }
 }
 

@@ -10,6 +10,7 @@ amplitude data the kernels update in place) bound to the configuration tensor
 it last saw; sampler, local energy and gradients share it.
 """
 import ctypes
+import math
 import weakref
 
 import torch
@@ -17,6 +18,20 @@ import torch.nn as nn
 
 from . import _lib
 from .walkers import pack, unpack
+
+# The reference's log-amplitude is log(clamp(|psi|, min=1e-45))
+# (vmc_torch/GPU/models/_base.py:101-109): zero and tiny amplitudes report this
+# floor, and their log-derivatives are zero (the clamp's gradient).  The
+# kernels keep the exact value (-inf for a singular orbital matrix) internally;
+# every log-amplitude handed back through the reference's interfaces is
+# floored the same way.
+LOG_MIN = math.log(1e-45)
+
+
+def floor_log(logabs):
+    """Copy of a log-amplitude vector with the reference's 1e-45 floor (NaN
+    stays NaN)."""
+    return logabs.clamp(min=LOG_MIN)
 
 
 class WalkerState:
@@ -44,6 +59,18 @@ class WalkerState:
 
     def bind(self, fxs):
         self.key = (weakref.ref(fxs), fxs._version, tuple(fxs.shape))
+
+    def view(self, a, b):
+        """Walkers a..b-1 as a state that shares this one's memory (every
+        per-walker tensor sliced along its first axis); unbound."""
+        v = WalkerState.__new__(WalkerState)
+        v.B, v.n_sites, v.device = b - a, self.n_sites, self.device
+        v.occ, v.sign, v.logabs, v.n_acc = self.occ[a:b], self.sign[a:b], self.logabs[a:b], self.n_acc[a:b]
+        v.key = None
+        v.param_key = self.param_key
+        v.extra = {k: (t[a:b] if isinstance(t, torch.Tensor) and t.dim() > 0 and t.shape[0] == self.B and k != "err"
+                       else t) for k, t in self.extra.items()}
+        return v
 
 
 class WavefunctionModel_GB300(nn.Module):
@@ -105,13 +132,52 @@ class WavefunctionModel_GB300(nn.Module):
         unpack(st.occ, self.n_sites, out=fxs)
         st.bind(fxs)
 
+    # ---- device status ----
+    def _err_word(self, st):
+        """Device status word of the state's kernels (None for models whose
+        kernels report through their return codes only)."""
+        return st.extra.get("err")
+
+    def _watch_err(self, st):
+        """Queue a copy of the status word to pinned host memory behind the
+        work just enqueued (no synchronisation)."""
+        err = self._err_word(st)
+        if err is None:
+            return
+        if "err_host" not in st.extra:
+            st.extra["err_host"] = torch.zeros(1, dtype=torch.int32, pin_memory=True)
+            st.extra["err_event"] = torch.cuda.Event()
+        st.extra["err_host"].copy_(err, non_blocking=True)
+        st.extra["err_event"].record(torch.cuda.current_stream(st.device))
+        st.extra["err_pending"] = True
+
+    def check_status(self, st, wait=False):
+        """Raise if a kernel of this state reported an error (a bounded device
+        wait that gave up, or configurations outside the model's sector).
+        wait=False looks only at a status copy that has already landed, so
+        the sampler never stalls the stream; wait=True reads the word now."""
+        err = self._err_word(st)
+        if err is None:
+            return
+        if wait:
+            v = int(err.item())
+        elif st.extra.get("err_pending") and st.extra["err_event"].query():
+            st.extra["err_pending"] = False
+            v = int(st.extra["err_host"].item())
+        else:
+            return
+        if v != 0:
+            err.zero_()
+            raise ValueError("%s kernel reported status %d: %s" % (type(self).__name__, v, _lib.message(v)))
+
     # ---- reference interface ----
     def forward_log(self, x):
         if x.shape[0] == 0:
             z = torch.zeros(0, dtype=torch.float64, device=x.device)
             return z, z.clone()
         st = self._eval_state(x)
-        return st.sign.clone(), st.logabs.clone()
+        self.check_status(st, wait=True)
+        return st.sign.clone(), floor_log(st.logabs)
 
     def forward(self, x):
         s, la = self.forward_log(x)
@@ -120,6 +186,13 @@ class WavefunctionModel_GB300(nn.Module):
     def log_amplitude(self, x, params_list=None):
         s, la = self.forward_log(x.reshape(1, -1))
         return s[0], la[0]
+
+    def take_singular_count(self):
+        """Walkers whose orbital matrix was found singular (zero amplitude)
+        since the last call; the count is reset.  Zero amplitudes are legal
+        states in the reference (its sampler and energy carry on), so they are
+        counted, not raised."""
+        return 0
 
     def amplitude(self, x, params_list=None):
         """Single-sample amplitude (the model's current parameters are used; the
@@ -189,6 +262,14 @@ class SlaterDeterminant_GB300(WavefunctionModel_GB300):
         if M.device != device:
             raise ValueError("model parameters must live on the walkers' device (call model.to(device))")
         return M.detach().contiguous()
+
+    def take_singular_count(self):
+        st = self._state
+        if st is None:
+            return 0
+        n = int(st.extra["nsing"].item())
+        st.extra["nsing"].zero_()
+        return n
 
     def _refresh(self, st, threshold):
         M = self._M(st.device)
@@ -335,12 +416,6 @@ class NNBF_GB300(WavefunctionModel_GB300):
         x["A"] = torch.empty((B, nf, nf), dtype=self._rdtype(), device=device)
         x["err"] = torch.zeros(1, dtype=torch.int32, device=device)
         return st
-
-    def _check_err(self, st):
-        if int(st.extra["err"].item()) != 0:
-            v = int(st.extra["err"].item())
-            st.extra["err"].zero_()
-            raise RuntimeError("NNBF kernel reported status %d (a bounded device wait gave up)" % v)
 
     def _refresh(self, st, threshold):
         ts, arr = self.net(st.device)

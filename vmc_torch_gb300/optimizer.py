@@ -3,10 +3,17 @@ with the reference's preconditioner / optimizer interfaces
 (vmc_torch/GPU/optimizer.py:130-251, 471-614, 884-907).
 
 minSR: O~ = (O - <O>)/sqrt(Ns); T = O~ O~^T + lambda I (Ns x Ns, FP64
-accumulation); Cholesky T = L L^T in FP64; x = T^-1 (E - <E>)/sqrt(Ns);
-dp = O~^T x.  The reference solves with torch.linalg.solve and falls back to
-lstsq (info = 1) when that raises; here a non-positive Cholesky pivot triggers
-one retry with the shift raised to 10 lambda + 1e-8 trace(T)/Ns and info = 1.
+accumulation); x = T^-1 (E - <E>)/sqrt(Ns); dp = O~^T x.  T is symmetric
+positive definite whenever lambda > 0 and O is finite, and is then factored by
+this library's FP64 Cholesky.  When the Cholesky meets a non-positive pivot (a
+negative or zero shift, a rank-deficient O) the solve follows the reference
+exactly (vmc_torch/GPU/optimizer.py:557-561): torch.linalg.solve (LU with
+partial pivoting) with info = 0, and when that raises on an exactly singular
+T, the minimum-norm least-squares solution with info = 1 (the role of the
+reference's lstsq; computed from the eigendecomposition of the symmetric T,
+eigenvalues below Ns * eps * max|eigenvalue| dropped).  These fallbacks are
+library calls on the failure path only; the Cholesky path never leaves this
+library's kernels.
 
 ``local_o`` may be a dense (Ns, Np) tensor (the reference's layout) or a
 :class:`FactoredO`, in which the NNBF output-layer block of every row is the
@@ -125,26 +132,26 @@ class MinSRGB300(PreconditionerGB300):
         _lib.call("vmc_sr_update", _lib.ptr(Oc), code, Ns, Np, Oc.stride(0), _lib.ptr(x), _lib.ptr(dp), s)
         return dp, time.time() - t0, info
 
-    # -- shared: Gram -> (shifted) FP64 Cholesky -> solve --
+    # -- shared: Gram -> FP64 Cholesky -> solve (reference fallbacks on failure) --
     @staticmethod
     def _factor_solve(build_gram, E, Ebar, Ns, shift, dev):
         s = _lib.stream_of(dev)
         T = torch.empty((Ns, Ns), dtype=torch.float64, device=dev)
-        info = 0
-        for attempt in range(2):
-            build_gram(T, shift)
-            flag = torch.zeros(1, dtype=torch.int32, device=dev)
-            _lib.call("vmc_sr_cholesky", _lib.ptr(T), Ns, Ns, _lib.ptr(flag), s)
-            if int(flag.item()) == 0:
-                break
-            info = 1
-            build_gram(T, 0.0)
-            tr = float(torch.diagonal(T).sum().item())
-            shift = 10.0 * shift + 1e-8 * tr / Ns
+        build_gram(T, shift)
+        flag = torch.zeros(1, dtype=torch.int32, device=dev)
+        _lib.call("vmc_sr_cholesky", _lib.ptr(T), Ns, Ns, _lib.ptr(flag), s)
         x = torch.empty(Ns, dtype=torch.float64, device=dev)
         _lib.call("vmc_sr_rhs", _lib.ptr(E), Ns, Ebar, _lib.ptr(x), s)
-        _lib.call("vmc_sr_cholesky_solve", _lib.ptr(T), Ns, Ns, _lib.ptr(x), s)
-        return x, info
+        if int(flag.item()) == 0:
+            _lib.call("vmc_sr_cholesky_solve", _lib.ptr(T), Ns, Ns, _lib.ptr(x), s)
+            return x, 0
+        # the factorisation overwrote T: rebuild it, then solve as the reference does
+        build_gram(T, shift)
+        T = torch.tril(T) + torch.tril(T, -1).t()   # symmetric from the lower triangle the kernels define
+        try:
+            return torch.linalg.solve(T, x), 0
+        except RuntimeError:
+            return _min_norm_solve(T, x), 1
 
     def _solve_factored(self, F, E, Ebar, n_params, shift, dev, run_sr, t0):
         s = _lib.stream_of(dev)
@@ -197,6 +204,16 @@ class MinSRGB300(PreconditionerGB300):
         _lib.call("vmc_gemm", 1, 0, Ng, Nh, Ns, 1.0 / rs, _lib.ptr(G), G.stride(0), _lib.ptr(H), H.stride(0),
                   _lib.ptr(xc), code, 1.0, _lib.ptr(dp_k), Nh, None, 0, 0, s)
         return F.assemble(dp_d, dp_k), time.time() - t0, info
+
+
+def _min_norm_solve(T, b):
+    """Minimum-norm least-squares solution of the symmetric system T x = b:
+    x = V diag(1/w) V^T b over the eigenpairs with |w| > Ns eps max|w| (the
+    cutoff numpy's lstsq uses for its singular values, which are |w| here)."""
+    w, V = torch.linalg.eigh(T)
+    cut = T.shape[0] * torch.finfo(T.dtype).eps * w.abs().max()
+    inv = torch.where(w.abs() > cut, 1.0 / w, torch.zeros_like(w))
+    return V @ (inv * (V.t() @ b))
 
 
 class OptimizerGB300:

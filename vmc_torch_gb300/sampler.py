@@ -12,6 +12,7 @@ host at ``new_flags.sum().item()``).
 import torch
 
 from . import _lib
+from .models import floor_log
 
 
 class SamplerGB300:
@@ -47,15 +48,17 @@ class MetropolisExchangeSpinfulSamplerGB300(SamplerGB300):
 
     def _run(self, fxs, model, graph, n_sweeps, use_log_amp, replay, instrument=None):
         st = model.bind_state(fxs)
+        model.check_status(st)   # a status copy of earlier work that has landed; never waits
         if instrument is None:
             model.sweep(st, graph, n_sweeps, self.seed, self.sweep_counter, self.hopping_rate, replay)
         else:
             model.sweep(st, graph, n_sweeps, self.seed, self.sweep_counter, self.hopping_rate, replay,
                         instrument=instrument)
+        model._watch_err(st)
         self.sweep_counter += n_sweeps
         model.store_configs(st, fxs)
         if use_log_amp:
-            return fxs, (st.sign.clone(), st.logabs.clone())
+            return fxs, (st.sign.clone(), floor_log(st.logabs))
         return fxs, st.sign * torch.exp(st.logabs)
 
     @torch.inference_mode()
