@@ -151,6 +151,7 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
+    world = int(os.environ.get("WORLD_SIZE", "1"))
     cores = os.cpu_count()
     for _ in range(args.warmup):
         cpu_port_rate(n_walkers=16, n_sweeps=1)
@@ -160,7 +161,7 @@ def run_reference(args):
         rates.append(r)
         tot += dt
     value = float(np.mean(rates))
-    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
             "config": workload_config({"sample": sample}), "impl": "reference",
@@ -500,6 +501,22 @@ def run_gb300(args):
     return 0
 
 
+def free_port():
+    import socket
+    with socket.socket() as so:
+        so.bind(("127.0.0.1", 0))
+        return so.getsockname()[1]
+
+
+def spawn_replicas(n, argv):
+    """``--gpus N`` outside a launcher: start N ranks of this script, one per
+    GPU, through torch.distributed.run on 127.0.0.1, and return the launcher's
+    exit status.  Each rank runs its own replica; rank 0 prints the line."""
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", str(n),
+           "--master-addr", "127.0.0.1", "--master-port", str(free_port()), os.path.abspath(__file__)] + list(argv)
+    return subprocess.call(cmd)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -517,6 +534,8 @@ def main():
     ap.add_argument("--walkers", type=int, default=B,
                     help="walkers per GPU (the headline workload uses 16384; smaller values are for profiling)")
     args = ap.parse_args()
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        return spawn_replicas(args.gpus, sys.argv[1:])
     globals()["B"] = args.walkers
     if args.warmup < 3:
         args.warmup = 3

@@ -18,7 +18,8 @@ from unittest import mock
 
 import numpy
 
-REFERENCE_ROOT = os.environ.get("VMC_REFERENCE_ROOT", "/root/reference")
+# the reference checkout to import from: required, no default location
+REFERENCE_ROOT = os.environ.get("VMC_REFERENCE_ROOT")
 _STUB = ("quimb", "symmray", "cotengra", "mpi4py", "pyblock2", "pyinstrument")
 
 
@@ -46,6 +47,9 @@ def install():
     global _installed
     if _installed:
         return
+    if not REFERENCE_ROOT or not os.path.isdir(os.path.join(REFERENCE_ROOT, "vmc_torch")):
+        raise RuntimeError("set VMC_REFERENCE_ROOT to a checkout of sjdu10/vmc_torch (the directory holding "
+                           "the vmc_torch package) to import the reference")
     import torch
 
     sys.meta_path.insert(0, _StubFinder())

@@ -1,9 +1,9 @@
 """Generate the golden fixtures in this directory from the REFERENCE's own code.
 
-Run in a container where the reference sources are readable (default
-/root/reference, override with VMC_REFERENCE_ROOT):
+Run where the reference sources are readable, naming their checkout in
+VMC_REFERENCE_ROOT (required):
 
-    python tests/golden/make_golden.py
+    VMC_REFERENCE_ROOT=<path to sjdu10/vmc_torch> python tests/golden/make_golden.py
 
 The reference is imported under the shims of ``oracle/refshim.py`` (its
 third-party TN/MPI dependencies are absent and are not on this path).  Every

@@ -45,7 +45,7 @@ def test_nan_parameters(kind):
     if kind == "slater":
         N, nup = 8, 4
         M = np.random.default_rng(0).normal(0, 0.1, (16, 8))
-        M[3, 5] = np.nan
+        M[:, 5] = np.nan   # a NaN column: every orbital matrix holds NaN
         m = vg.SlaterDeterminant_GB300(16, 8).to(DEV)
         with torch.no_grad():
             m.params[0].copy_(torch.as_tensor(M))
@@ -229,7 +229,7 @@ def test_occupation_outside_the_lattice_is_reported():
     keep = np.arange(R) != 5
     assert np.median(np.abs(la.cpu().numpy()[keep] - lo[keep])) < 2e-3
     # through the model interface the same state raises
-    st = m._new_state(R, torch.device(DEV))
+    st = m._new_state(R, occ.device)
     st.occ.copy_(occ)
     m._refresh(st, 0)
     with pytest.raises(ValueError, match="status 1"):

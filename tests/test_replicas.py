@@ -48,3 +48,24 @@ def test_replica_rate_single_process():
     import bench
     rate, ms = bench.replica_rate(500, 5.0)
     assert ms == 5.0 and rate == pytest.approx(1e5)
+
+
+@pytest.mark.timeout(600)
+def test_bench_gpus_2_spawns_two_ranks():
+    """``bench.py --gpus 2`` outside a launcher starts two ranks itself (one
+    per GPU); on the reference arm, which runs on the host CPU, rank 0 alone
+    prints the line and reports both ranks."""
+    import json
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ)
+    for k in ("WORLD_SIZE", "RANK", "LOCAL_RANK", "MASTER_ADDR", "MASTER_PORT"):
+        env.pop(k, None)
+    r = subprocess.run([sys.executable, os.path.join(root, "bench.py"), "--impl", "reference", "--gpus", "2",
+                        "--steps", "1", "--warmup", "3"], capture_output=True, text=True, env=env, timeout=580)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0

@@ -1419,6 +1419,8 @@ struct StageTimer {
     used = 0;
   }
 };
+// One timer for the process: stage timing (vmc_nnbf_sweep with stage_ms) is
+// a benchmarking aid and is not re-entrant across host threads.
 StageTimer g_timer;
 #define STAGE_BEGIN(s) g_timer.mark((s), true)
 #define STAGE_END(s) g_timer.mark((s), false)
@@ -1427,15 +1429,23 @@ StageTimer g_timer;
 // small enough to stay resident in L2 between the GEMM epilogue and the LU.
 constexpr int64_t kChunkRows = 4096;
 
-int g_num_sms = 0;
+// Per-device state is indexed by the current device's ordinal, so that one
+// process may drive several GPUs.
+constexpr int kMaxDevices = 64;
+int g_num_sms[kMaxDevices] = {};
+int current_device() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return 0;
+  return dev;
+}
 int num_sms() {
-  if (!g_num_sms) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
-    if (g_num_sms <= 0) g_num_sms = 148;
+  const int dev = current_device();
+  if (!g_num_sms[dev]) {
+    int n = 0;
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    g_num_sms[dev] = n > 0 ? n : 148;
   }
-  return g_num_sms;
+  return g_num_sms[dev];
 }
 
 void set_attrs();
@@ -1610,13 +1620,18 @@ int launch_eval_rows(int prec, int64_t R, int N, int nf, const uint64_t* row_occ
   return VMC_OK;
 }
 
-bool g_attr_done = false;
+// Kernel attributes are per device: set once on each device the first time
+// that device is current.
+bool g_attr_done[kMaxDevices] = {};
+std::mutex g_attr_mu;
 void set_attrs() {
-  if (g_attr_done) return;
+  const int dev = current_device();
+  std::lock_guard<std::mutex> lk(g_attr_mu);
+  if (g_attr_done[dev]) return;
   cudaFuncSetAttribute(k_gemm_tc<EPI_GELU_BF16>, cudaFuncAttributeMaxDynamicSharedMemorySize, GEMM_SMEM);
   cudaFuncSetAttribute(k_gemm_tc<EPI_BACKFLOW>, cudaFuncAttributeMaxDynamicSharedMemorySize, GEMM_SMEM);
   cudaFuncSetAttribute(k_backflow_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize, PB_SMEM);
-  g_attr_done = true;
+  g_attr_done[dev] = true;
 }
 
 int check_shape(int prec, int N, int nf, int hidden) {
