@@ -192,6 +192,14 @@ int vmc_nnbf_mh_step(const void* const* net_ptrs, int n_sites, int nf, int hidde
                      int64_t B, const uint64_t* prop_occ, const void* rec4, void* z0, void* z0p, double* sign,
                      double* logabs, int32_t* n_acc, void* H1, void* H2, void* A, float* lg_x, const float* lg_p,
                      int* kstats, int* d_err, void* stream);
+/* MH accept of learned proposals for any model (the proposals' sign_p /
+ * logabs_p (B) come from the caller's own evaluation of prop_occ): accept with
+ * min(1, |psi'/psi|^2 q(x'->x)/q(x->x')), a NaN ratio never; on accept the
+ * walker takes x', sign, logabs and (lg_x / lg_p, both or neither) the
+ * proposal logits at x'.  n_acc (B) and kstats[8] are nullable counters. */
+int vmc_accept_mh(uint64_t* occ, int64_t B, const uint64_t* prop_occ, const void* rec4, const double* sign_p,
+                  const double* logabs_p, double* sign, double* logabs, int32_t* n_acc, float* lg_x,
+                  const float* lg_p, int* kstats, void* stream);
 /* Training (FP32 CUDA cores): forward, masked softmax cross entropy against the
  * heat-bath hop targets tgt (R, 2E) and the k target ktgt (4), backward, Adam.
  * params/grad/m1/m2: flat FP32 [W1, b1, W2, b2, Wo, bo]; ws: R*(4*512+2*256) f32;

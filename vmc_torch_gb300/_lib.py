@@ -51,6 +51,7 @@ SIGNATURES = {
     "vmc_prop_logits": [P, I32, P, I64, P, P, P, P, P, P],
     "vmc_prop_sample": [P, I32, I32, P, P, I64, U64, U64, P, P, P],
     "vmc_prop_reverse": [P, I32, I32, P, P, I64, P, P],
+    "vmc_accept_mh": [P, I64, P, P, P, P, P, P, P, P, P, P, P],
     "vmc_nnbf_mh_step": [P, I32, I32, I32, F64, P, I64, P, P, P, P, P, P, P, P, P, P, P, P, P, P, P],
     "vmc_prop_train_step": [I32, P, I32, P, I32, P, P, P, F32, P, P, P, P, I64, F32, F32, F32, F32, I32, P, P, P],
     "vmc_prop_inputs_f32": [I32, P, I64, P, P],

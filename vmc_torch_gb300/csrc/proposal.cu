@@ -382,29 +382,33 @@ __global__ void k_prop_reverse(int64_t B, Lat L, const float* __restrict__ logit
 // ---------------------------------------------------------------------------
 // training: FP32 CUDA cores
 // C[M x N] = op(A) op(B) (+ bias[n]); row-major; EPI: 0 plain, 1 gelu(pre) with
-// pre stored in aux, 2 accumulate (C += ...)
+// pre stored in aux, 2 accumulate (C += ...), 3 split-K: block z adds the
+// partial product over k in [z kchunk, (z+1) kchunk) to C atomically (C
+// cleared beforehand; used for the weight gradients, whose K is the batch).
 template <int EPI>
 __global__ void k_sgemm(int ta, int tb, int M, int N, int K, const float* __restrict__ A, int lda,
                         const float* __restrict__ Bm, int ldb, const float* __restrict__ bias, float* __restrict__ C,
-                        int ldc, float* __restrict__ aux) {
+                        int ldc, float* __restrict__ aux, int kchunk) {
   constexpr int T = 64, TKk = 16;
   __shared__ float As[TKk][T + 1];
   __shared__ float Bs[TKk][T + 1];
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
   const int m0 = blockIdx.y * T, n0 = blockIdx.x * T;
+  const int kb = EPI == 3 ? blockIdx.z * kchunk : 0;
+  const int ke = EPI == 3 ? min(K, kb + kchunk) : K;
   float acc[4][4] = {};
-  for (int k0 = 0; k0 < K; k0 += TKk) {
+  for (int k0 = kb; k0 < ke; k0 += TKk) {
     for (int idx = threadIdx.x; idx < T * TKk; idx += 256) {
       int r, kk;
       if (ta) { kk = idx / T; r = idx - kk * T; } else { r = idx / TKk; kk = idx - r * TKk; }
       const int gm = m0 + r, gk = k0 + kk;
-      As[kk][r] = (gm < M && gk < K) ? (ta ? A[(size_t)gk * lda + gm] : A[(size_t)gm * lda + gk]) : 0.f;
+      As[kk][r] = (gm < M && gk < ke) ? (ta ? A[(size_t)gk * lda + gm] : A[(size_t)gm * lda + gk]) : 0.f;
     }
     for (int idx = threadIdx.x; idx < T * TKk; idx += 256) {
       int c, kk;
       if (tb) { c = idx / TKk; kk = idx - c * TKk; } else { kk = idx / T; c = idx - kk * T; }
       const int gn = n0 + c, gk = k0 + kk;
-      Bs[kk][c] = (gn < N && gk < K) ? (tb ? Bm[(size_t)gn * ldb + gk] : Bm[(size_t)gk * ldb + gn]) : 0.f;
+      Bs[kk][c] = (gn < N && gk < ke) ? (tb ? Bm[(size_t)gn * ldb + gk] : Bm[(size_t)gk * ldb + gn]) : 0.f;
     }
     __syncthreads();
 #pragma unroll
@@ -429,6 +433,7 @@ __global__ void k_sgemm(int ta, int tb, int M, int N, int K, const float* __rest
       const size_t o = (size_t)gm * ldc + gn;
       if (EPI == 1) { aux[o] = v; C[o] = gelu_f(v); }
       else if (EPI == 2) C[o] += v;
+      else if (EPI == 3) atomicAdd(&C[o], v);
       else C[o] = v;
     }
 }
@@ -562,7 +567,61 @@ int gemm_bf16(int epi, const __nv_bfloat16* A, int64_t M, int K, const __nv_bflo
 
 }  // namespace
 
+// Metropolis-Hastings accept of learned proposals for any model: the
+// proposals' sign / log-amplitude come from the model's own evaluation.
+// Accept with min(1, |psi'/psi|^2 q(x'->x)/q(x->x')); a NaN ratio never
+// accepts, a zero-amplitude proposal never, and from a zero-amplitude walker
+// every non-zero proposal with a finite reverse probability does.  On accept
+// the walker takes x', its sign / log-amplitude and (when given) the proposal
+// logits at x'.  One warp per walker (the logits row is 256 floats).
+__global__ void k_accept_mh(int64_t B, uint64_t* __restrict__ occ, const uint64_t* __restrict__ prop_occ,
+                            const PropRec4* __restrict__ rec, const double* __restrict__ sign_p,
+                            const double* __restrict__ logabs_p, double* __restrict__ sign, double* __restrict__ logabs,
+                            int32_t* __restrict__ n_acc, float* __restrict__ lg_x, const float* __restrict__ lg_p,
+                            int* __restrict__ kstats) {
+  const int lane = threadIdx.x & 31;
+  const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (w >= B) return;
+  const PropRec4 r = rec[w];
+  if (!r.flag) return;
+  const double l1 = logabs_p[w], l0 = logabs[w];
+  const double lr = 2.0 * (l1 - l0) + ((double)r.logq_rev - (double)r.logq_fwd);
+  bool acc;
+  if (!(l1 > -INFINITY) || sign_p[w] == 0.0 || !isfinite(r.logq_rev)) acc = false;
+  else if (l0 == -INFINITY) acc = true;
+  else acc = (lr == lr) && ((double)r.u_acc < exp(fmin(lr, 80.0)));
+  const int kk = min(max(r.k, 1), 4) - 1;
+  if (kstats && lane == 0) {
+    atomicAdd(&kstats[kk], 1);
+    if (acc) atomicAdd(&kstats[4 + kk], 1);
+  }
+  if (!acc) return;
+  if (lg_x) {
+#pragma unroll
+    for (int q = 0; q < 8; ++q) lg_x[w * PLOG + lane * 8 + q] = lg_p[w * PLOG + lane * 8 + q];
+  }
+  if (lane == 0) {
+    occ[2 * w] = prop_occ[2 * w];
+    occ[2 * w + 1] = prop_occ[2 * w + 1];
+    sign[w] = sign_p[w];
+    logabs[w] = l1;
+    if (n_acc) n_acc[w] += 1;
+  }
+}
+
 extern "C" {
+
+int vmc_accept_mh(uint64_t* occ, int64_t B, const uint64_t* prop_occ, const void* rec4, const double* sign_p,
+                  const double* logabs_p, double* sign, double* logabs, int32_t* n_acc, float* lg_x,
+                  const float* lg_p, int* kstats, void* stream) {
+  if (B < 0 || (lg_x != nullptr) != (lg_p != nullptr)) return VMC_ERR_ARGS;
+  if (B == 0) return VMC_OK;
+  if (!occ || !prop_occ || !rec4 || !sign_p || !logabs_p || !sign || !logabs) return VMC_ERR_ARGS;
+  k_accept_mh<<<(unsigned)((B * 32 + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
+      B, occ, prop_occ, (const PropRec4*)rec4, sign_p, logabs_p, sign, logabs, n_acc, lg_x, lg_p, kstats);
+  VMC_CUDA_CHECK_LAUNCH();
+  return VMC_OK;
+}
 
 // Inference: logits (R, 256) fp32 for configurations occ (R, 2).
 // wts[6]: W1 (512, Kin) bf16, b1 (512) f32, W2 (512, 512) bf16, b2 f32,
@@ -646,24 +705,31 @@ int vmc_prop_train_step(int n_sites, const int32_t* edges, int n_edges, const ui
   float* LG = H2 + (size_t)R * PH;      // R x 256 logits
   float* DL = LG + (size_t)R * PLOG;    // R x 256 dlogits
   auto grid = [](int M, int N) { return dim3((unsigned)((N + 63) / 64), (unsigned)((M + 63) / 64)); };
+  // weight gradients: K = R (the batch), split in chunks of 256 rows so that
+  // the 512 x 512 products fill the GPU; the partial sums land atomically in
+  // the cleared gradient vector
+  const int kc = 256;
+  const unsigned nz = (unsigned)((R + kc - 1) / kc);
+  auto gridk = [nz](int M, int N) { return dim3((unsigned)((N + 63) / 64), (unsigned)((M + 63) / 64), nz); };
+  if (cudaMemsetAsync(grad, 0, (size_t)np * sizeof(float), st) != cudaSuccess) return VMC_ERR_CUDA;
   // forward
-  k_sgemm<1><<<grid(R, PH), 256, 0, st>>>(0, 1, R, PH, Kin, Xf, Kin, W1, Kin, b1, H1, PH, Z1);
-  k_sgemm<1><<<grid(R, PH), 256, 0, st>>>(0, 1, R, PH, PH, H1, PH, W2, PH, b2, H2, PH, Z2);
-  k_sgemm<0><<<grid(R, PLOG), 256, 0, st>>>(0, 1, R, PLOG, PH, H2, PH, Wo, PH, bo, LG, PLOG, nullptr);
+  k_sgemm<1><<<grid(R, PH), 256, 0, st>>>(0, 1, R, PH, Kin, Xf, Kin, W1, Kin, b1, H1, PH, Z1, 0);
+  k_sgemm<1><<<grid(R, PH), 256, 0, st>>>(0, 1, R, PH, PH, H1, PH, W2, PH, b2, H2, PH, Z2, 0);
+  k_sgemm<0><<<grid(R, PLOG), 256, 0, st>>>(0, 1, R, PLOG, PH, H2, PH, Wo, PH, bo, LG, PLOG, nullptr, 0);
   Lat L{edges, n_edges, n_sites};
   k_prop_loss<<<(unsigned)((R * 32 + 255) / 256), 256, 0, st>>>(R, L, occ, LG, tgt, ktgt, kweight, DL, loss);
   // backward
-  k_sgemm<0><<<grid(PLOG, PH), 256, 0, st>>>(1, 0, PLOG, PH, R, DL, PLOG, H2, PH, nullptr, gWo, PH, nullptr);
+  k_sgemm<3><<<gridk(PLOG, PH), 256, 0, st>>>(1, 0, PLOG, PH, R, DL, PLOG, H2, PH, nullptr, gWo, PH, nullptr, kc);
   k_colsum<<<(PLOG + 255) / 256, 256, 0, st>>>(R, PLOG, DL, PLOG, gbo);
   // dH2 = DL Wo -> stored in H2 (H2 no longer needed), then * gelu'(Z2)
-  k_sgemm<0><<<grid(R, PH), 256, 0, st>>>(0, 0, R, PH, PLOG, DL, PLOG, Wo, PH, nullptr, H2, PH, nullptr);
+  k_sgemm<0><<<grid(R, PH), 256, 0, st>>>(0, 0, R, PH, PLOG, DL, PLOG, Wo, PH, nullptr, H2, PH, nullptr, 0);
   k_gelu_back<<<(unsigned)(((int64_t)R * PH + 255) / 256), 256, 0, st>>>((int64_t)R * PH, Z2, H2);
-  k_sgemm<0><<<grid(PH, PH), 256, 0, st>>>(1, 0, PH, PH, R, H2, PH, H1, PH, nullptr, gW2, PH, nullptr);
+  k_sgemm<3><<<gridk(PH, PH), 256, 0, st>>>(1, 0, PH, PH, R, H2, PH, H1, PH, nullptr, gW2, PH, nullptr, kc);
   k_colsum<<<(PH + 255) / 256, 256, 0, st>>>(R, PH, H2, PH, gb2);
   // dH1 = dZ2 W2 -> Z2 buffer, * gelu'(Z1)
-  k_sgemm<0><<<grid(R, PH), 256, 0, st>>>(0, 0, R, PH, PH, H2, PH, W2, PH, nullptr, Z2, PH, nullptr);
+  k_sgemm<0><<<grid(R, PH), 256, 0, st>>>(0, 0, R, PH, PH, H2, PH, W2, PH, nullptr, Z2, PH, nullptr, 0);
   k_gelu_back<<<(unsigned)(((int64_t)R * PH + 255) / 256), 256, 0, st>>>((int64_t)R * PH, Z1, Z2);
-  k_sgemm<0><<<grid(PH, Kin), 256, 0, st>>>(1, 0, PH, Kin, R, Z2, PH, Xf, Kin, nullptr, gW1, Kin, nullptr);
+  k_sgemm<3><<<gridk(PH, Kin), 256, 0, st>>>(1, 0, PH, Kin, R, Z2, PH, Xf, Kin, nullptr, gW1, Kin, nullptr, kc);
   k_colsum<<<(PH + 255) / 256, 256, 0, st>>>(R, PH, Z2, PH, gb1);
   // Adam
   const float c1 = 1.0f - powf(beta1, (float)t), c2 = 1.0f - powf(beta2, (float)t);

@@ -19,10 +19,12 @@ only (vmc_torch/GPU/sampler.py:47-137); plain Metropolis stays available as the
 fallback and as the baseline that judges this proposal (tau_int of E_loc).
 """
 import math
+import time
 
 import torch
 
 from . import _lib
+from .models import floor_log
 from .sampler import SamplerGB300
 
 PH, PLOG, KMAX = 512, 256, 4
@@ -194,9 +196,12 @@ class LearnedProposal:
 
 class LearnedSamplerGB300(SamplerGB300):
     """Metropolis-Hastings sampler with the learned proposal.  One ``step``
-    performs ``moves_per_step`` learned MH moves per walker (the mixed NNBF
-    model evaluates every proposal); it mutates ``fxs`` in place like the
-    reference sampler."""
+    performs ``moves_per_step`` learned MH moves per walker; it mutates
+    ``fxs`` in place like the reference sampler.  The mixed-precision NNBF
+    model evaluates and accepts the proposals in one fused call
+    (vmc_nnbf_mh_step); any other model evaluates them with its own kernels
+    and the walkers move by the model-agnostic vmc_accept_mh, after which the
+    model's per-walker state is rebuilt for the new configurations."""
 
     def __init__(self, proposal, moves_per_step=112):
         self.proposal = proposal
@@ -210,12 +215,41 @@ class LearnedSamplerGB300(SamplerGB300):
 
     GROUP = 4096   # walkers per group when the batch is split over streams
 
+    @staticmethod
+    def _native(model):
+        return getattr(model, "precision", None) == "mixed" and hasattr(model, "mh_step")
+
+    def _generic_moves(self, st, model):
+        P = self.proposal
+        B = st.B
+        key = (id(model), B, str(st.device))
+        if getattr(self, "_tmp_key", None) != key:
+            self._tmp = model._new_state(B, st.device)
+            self._tmp_key = key
+        tmp = self._tmp
+        Lx = P.logits(st.occ).clone()
+        s = _lib.stream_of(st.device)
+        for _ in range(self.moves_per_step):
+            prop, rec, Lp = P.propose(st.occ, Lx)
+            tmp.occ.copy_(prop)
+            model._refresh(tmp, 0)
+            _lib.call("vmc_accept_mh", _lib.ptr(st.occ), B, _lib.ptr(prop), _lib.ptr(rec), _lib.ptr(tmp.sign),
+                      _lib.ptr(tmp.logabs), _lib.ptr(st.sign), _lib.ptr(st.logabs), _lib.ptr(st.n_acc),
+                      _lib.ptr(Lx), _lib.ptr(Lp), _lib.ptr(P.kstats), s)
+        model._refresh(st, 0)   # the model's per-walker state for the configurations reached
+
     @torch.inference_mode()
     def step(self, fxs, model, graph=None, use_log_amp=False, **kwargs):
         st = model.bind_state(fxs)
         P = self.proposal
         B = st.B
         P._work(B)
+        if not self._native(model):
+            self._generic_moves(st, model)
+            model.store_configs(st, fxs)
+            if use_log_amp:
+                return fxs, (st.sign.clone(), floor_log(st.logabs))
+            return fxs, st.sign * torch.exp(st.logabs)
         Lx = P.logits(st.occ).clone()   # logits at the current configurations
         if B < 2 * self.GROUP:
             for _ in range(self.moves_per_step):
@@ -237,7 +271,42 @@ class LearnedSamplerGB300(SamplerGB300):
                         model.mh_step(st, prop, rec, Lx[a:b], Lp, P.kstats, rows=(a, b))
             for s in streams:
                 main.wait_stream(s)
+        model._watch_err(st)
         model.store_configs(st, fxs)
         if use_log_amp:
-            return fxs, (st.sign.clone(), st.logabs.clone())
+            return fxs, (st.sign.clone(), floor_log(st.logabs))
         return fxs, st.sign * torch.exp(st.logabs)
+
+
+class OnlineProposalTraining:
+    """Online training schedule of the learned proposal inside a VMC loop, as
+    an ``on_step_end(info)`` callback of either driver (``VMC_GB300.run_vmc_loop``
+    or the reference's ``VMC_GPU.run_vmc_loop``, vmc_torch/GPU/VMC.py:645-847):
+    after every SR step the step's samples and their heat-bath hop targets
+    (from that step's local-energy pass) join the proposal's ring buffer (its
+    last ``buffer`` samples), and every ``every`` steps the proposal trains
+    for ``epochs`` epochs over the buffer.  ``then`` is called afterwards with
+    the same info (to chain the caller's own callback).  ``train_seconds``
+    accumulates the training wall time (synchronised) for the ESS accounting."""
+
+    def __init__(self, proposal, model, every=10, epochs=2, batch=4096, then=None):
+        self.proposal, self.model = proposal, model
+        self.every, self.epochs, self.batch = int(every), int(epochs), int(batch)
+        self.then = then
+        self.steps = 0
+        self.sessions = 0
+        self.train_seconds = 0.0
+        self.last_loss = None
+
+    def __call__(self, info):
+        self.proposal.record(self.model)
+        self.steps += 1
+        if self.steps % self.every == 0:
+            torch.cuda.synchronize(self.proposal.device)
+            t0 = time.time()
+            self.last_loss = self.proposal.train(epochs=self.epochs, batch=self.batch)
+            torch.cuda.synchronize(self.proposal.device)
+            self.train_seconds += time.time() - t0
+            self.sessions += 1
+        if self.then is not None:
+            self.then(info)
