@@ -84,9 +84,11 @@ def test_learned_sampler_is_stationary_on_4x2():
     print("4x2, %d samples: learned chi2/dof %.2f TV %.4f (acceptance %.3f, k mix %s); plain chi2/dof %.2f TV %.4f"
           % (counts.sum(), chi2 / dof, tv, acc, np.round(kk, 3), chi2c / dof, tvc))
     assert acc > 0.05 and kk[1:].sum() > 0.3   # multi-hop moves are proposed and accepted
-    # snapshots one step apart are weakly correlated: chi2 up to 4x its dof
-    assert chi2 / dof < 4.0 and tv < 0.01
-    assert chi2c / dof < 4.0
+    # snapshots one step apart are weakly correlated: chi2 up to 4x its dof; at
+    # 1e6 samples over 4900 states the total variation is sampling noise
+    # (~0.02), so it is held to the plain control's
+    assert chi2 / dof < 4.0 and chi2c / dof < 4.0
+    assert tv < 1.5 * tvc + 0.005
 
 
 def _nnbf_6x6(seed=7):

@@ -138,6 +138,7 @@ class WavefunctionModel_GB300(nn.Module):
         kernels report through their return codes only)."""
         return st.extra.get("err")
 
+    @torch.inference_mode()
     def _watch_err(self, st):
         """Queue a copy of the status word to pinned host memory behind the
         work just enqueued (no synchronisation)."""
@@ -151,6 +152,7 @@ class WavefunctionModel_GB300(nn.Module):
         st.extra["err_event"].record(torch.cuda.current_stream(st.device))
         st.extra["err_pending"] = True
 
+    @torch.inference_mode()
     def check_status(self, st, wait=False):
         """Raise if a kernel of this state reported an error (a bounded device
         wait that gave up, or configurations outside the model's sector).
@@ -263,6 +265,7 @@ class SlaterDeterminant_GB300(WavefunctionModel_GB300):
             raise ValueError("model parameters must live on the walkers' device (call model.to(device))")
         return M.detach().contiguous()
 
+    @torch.inference_mode()
     def take_singular_count(self):
         st = self._state
         if st is None:
