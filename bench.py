@@ -271,67 +271,159 @@ def peps_block(dev, steps, fp32_peak_tflops, cpu=True, env_reuse=True):
 
 
 # ---------------------------------------------------------------------------
-def ess_compare(model, H, fxs, dev, samples=160, moves=28, train_steps=4, epochs=8, discard=16):
+def ess_block(dev, n_walkers, samples=160, discard=16, moves=28, sr_steps=20, pre_walkers=4096, every=10, epochs=2,
+              lr=0.02):
     """ESS/s of E_loc for plain exchange/hop Metropolis (one 112-edge sweep per
-    sample) vs the learned proposal (``moves`` MH moves per sample), from the
-    same equilibrated walkers at the same parameters.  The proposal is first
-    trained on ``train_steps`` x B plain-chain samples.  ESS/s counts sampler
-    device time (CUDA events); local energies are evaluated after every sample
-    for the estimator and are not part of either sampler's time.  The first
-    ``discard`` samples of each chain are left out of the estimates."""
+    sample) vs the learned proposal (``moves`` MH moves per sample) on the 8x8
+    backflow model after ``sr_steps`` SR steps (not at random init).
+
+    Schedule: the SR steps run on ``pre_walkers`` walkers with the plain
+    sampler; the learned proposal records every step's samples (ring buffer of
+    the last 65536) and trains ``epochs`` epochs every ``every`` steps (the
+    OnlineProposalTraining hook).  Then, at the final parameters, both
+    samplers draw ``samples`` samples per chain from the same equilibrated
+    ``n_walkers`` walkers (the first ``discard`` left out of the estimates).
+    ESS/s is reported three ways: (a) sampler device time only; (b) with the
+    proposal's training charged as on the schedule, one session per ``every``
+    samples (one sample per chain per SR step); (c) with the local-energy
+    device time of every sample added to both samplers; and (b)+(c)."""
     import torch
     import vmc_torch_gb300 as vg
-    from vmc_torch_gb300.proposal import LearnedProposal, LearnedSamplerGB300
+    from vmc_torch_gb300.proposal import LearnedProposal, LearnedSamplerGB300, OnlineProposalTraining
     from vmc_torch_gb300.stats import split_rhat, tau_int
 
+    model = vg.NNBF_GB300(LX * LY, NUP + NDN, hidden_dim=HID, n_layers=2, bf_scale=BF_SCALE, precision="mixed",
+                          generator=torch.Generator().manual_seed(4321)).to(dev)
+    H = vg.spinful_Fermi_Hubbard_square_lattice_torch(LX, LY, 1.0, 8.0, NUP + NDN, n_fermions_per_spin=(NUP, NDN))
+    H.precompute_hops_gpu(dev)
     graph = H.graph
-    plain = vg.MetropolisExchangeSpinfulSamplerGB300(seed=101)
     prop = LearnedProposal(LX * LY, H.edges_on(dev), device=dev, seed=5)
-    x = fxs.clone()
-    for _ in range(train_steps):
-        plain.step(x, model, graph)
-        vg.evaluate_energy(x, model, H)
-        prop.record(model)
+    hook = OnlineProposalTraining(prop, model, every=every, epochs=epochs, batch=4096)
+    plain = vg.MetropolisExchangeSpinfulSamplerGB300(seed=303)
+    xp = vg.init_walkers(pre_walkers, LX * LY, NUP, NDN, seed=77, device=dev)
+    cfg = vg.VMCLoopConfig(vmc_steps=sr_steps, ns_per_rank=pre_walkers, grad_batch_size=pre_walkers,
+                           n_params=model.n_params, nsites=LX * LY, learning_rate=lr, diag_shift=1e-3,
+                           burn_in_steps=10, factored_o=True)
+    drv = vg.VMC_GB300(plain, vg.MinSRGB300(), vg.SGDGB300(lr))
     t0 = time.time()
-    loss = None
-    for _ in range(epochs):
-        loss = prop.train(epochs=1, batch=4096)
+    hist, xp = drv.run_vmc_loop(xp, model, H, graph, 0, 1, cfg, on_step_end=hook)
     torch.cuda.synchronize()
-    t_train = time.time() - t0
+    t_pre = time.time() - t0
+    t_train = hook.train_seconds / max(hook.sessions, 1)
+
+    x = vg.init_walkers(n_walkers, LX * LY, NUP, NDN, seed=78, device=dev)
+    plain.burn_in(x, model, graph, 8)
     learned = LearnedSamplerGB300(prop, moves_per_step=moves)
 
     def run(sampler, x0):
         xc = x0.clone()
-        Es, tsum = [], 0.0
+        Es, ts, te = [], 0.0, 0.0
         for _ in range(samples):
-            torch.cuda.synchronize()
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record()
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+            ev[0].record()
             sampler.step(xc, model, graph)
-            e1.record()
-            torch.cuda.synchronize()
-            tsum += e0.elapsed_time(e1) / 1e3
+            ev[1].record()
             Es.append(vg.evaluate_energy(xc, model, H)[1])
+            ev[2].record()
+            torch.cuda.synchronize()
+            ts += ev[0].elapsed_time(ev[1]) / 1e3
+            te += ev[1].elapsed_time(ev[2]) / 1e3
         E = torch.stack(Es[discard:]).t().contiguous()
         tau = tau_int(E)
         nb, used = E.shape
-        t_used = tsum * used / samples
-        return {"ess_per_s": nb * used / tau / t_used, "tau_int_samples": tau, "sampler_s": tsum,
-                "ms_per_sample": 1e3 * tsum / samples, "energy_per_site": float(E.mean().item()) / (LX * LY),
+        ess = nb * used / tau
+        f = used / samples
+        return {"tau_int_samples": tau, "ess": ess, "sampler_s": ts, "eloc_s": te,
+                "ms_per_sample": 1e3 * ts / samples, "eloc_ms_per_sample": 1e3 * te / samples,
+                "ess_per_s": ess / (ts * f), "ess_per_s_with_eloc": ess / ((ts + te) * f),
+                "energy_per_site": float(E.mean().item()) / (LX * LY),
                 "stderr_per_site": float(E.std().item()) / (LX * LY) * (tau / (nb * used)) ** 0.5,
                 "split_rhat": split_rhat(E)}
 
     rp = run(plain, x)
     rl = run(learned, x)
+    # (b): one training session per `every` samples, counted over the samples the estimate uses
+    used_frac = (samples - discard) / samples
+    train_s = (samples / every) * t_train * used_frac
+    rl["ess_per_s_with_training"] = rl["ess"] / (rl["sampler_s"] * used_frac + train_s)
+    rl["ess_per_s_with_training_and_eloc"] = rl["ess"] / ((rl["sampler_s"] + rl["eloc_s"]) * used_frac + train_s)
+    rp["ess_per_s_with_training"] = rp["ess_per_s"]
+    rp["ess_per_s_with_training_and_eloc"] = rp["ess_per_s_with_eloc"]
     acc = float((prop.k_acc.sum() / prop.k_prop.sum().clamp_min(1)).item())
     dE = abs(rp["energy_per_site"] - rl["energy_per_site"])
-    return {"plain": rp, "learned": rl, "ess_ratio_learned_over_plain": rl["ess_per_s"] / rp["ess_per_s"],
+    ratio = {k: rl[k] / rp[k] for k in ("ess_per_s", "ess_per_s_with_training", "ess_per_s_with_eloc",
+                                        "ess_per_s_with_training_and_eloc")}
+    return {"plain": rp, "learned": rl,
+            "ratio_learned_over_plain": {"a_sampler_only": ratio["ess_per_s"],
+                                         "b_with_training_schedule": ratio["ess_per_s_with_training"],
+                                         "c_with_local_energy": ratio["ess_per_s_with_eloc"],
+                                         "b_and_c": ratio["ess_per_s_with_training_and_eloc"]},
+            "ess_ratio_learned_over_plain": ratio["ess_per_s"],
             "abs_dE_per_site": dE, "matched_energy_1e-3": dE < 1e-3,
             "dE_sigma": dE / (rp["stderr_per_site"] ** 2 + rl["stderr_per_site"] ** 2) ** 0.5,
-            "samples_per_chain": samples, "discarded_per_chain": discard, "learned_moves_per_sample": moves, "learned_acceptance": acc,
-            "proposal_train_loss": loss, "proposal_train_s": t_train,
+            "walkers": n_walkers, "samples_per_chain": samples, "discarded_per_chain": discard,
+            "learned_moves_per_sample": moves, "learned_acceptance": acc,
+            "wavefunction": {"sr_steps_before_measuring": sr_steps, "sr_walkers": pre_walkers, "lr": lr,
+                             "diag_shift": 1e-3, "energy_per_site_first_last": [hist[0], hist[-1]],
+                             "seconds": t_pre},
+            "training": {"schedule": "every %d SR steps, %d epochs over the last %d samples" % (every, epochs, prop.cap),
+                         "sessions": hook.sessions, "seconds_per_session": t_train, "last_loss": hook.last_loss},
             "proposal": "MLP 128->512->512 GELU (BF16 tcgen05 inference, FP32 CUDA-core training), k<=4 hops"}
+
+
+# ---------------------------------------------------------------------------
+def sr_block(model, H, fxs, dev, fp32_peak_tflops, diag_shift=1e-4):
+    """Configs 2-3's SR path at the headline size: the hand-written adjoint O
+    (dense block + Kronecker factors of the out_w block) for every walker, the
+    local energies, then minSR (centring, dense Gram on FP32 CUDA cores with
+    compensated accumulation, the Kronecker-corrected head block, FP64
+    Cholesky, solves, update).  Device time per stage (CUDA events on the
+    current stream) and the algorithmic FLOP of each: dense Gram
+    2 Ns^2 Np_dense, head 2 Ns^2 (2N nf + 256) (+ the mean 2 Ns 2N nf 256),
+    Cholesky Ns^3 / 3."""
+    import torch
+    import vmc_torch_gb300 as vg
+    stream = torch.cuda.current_stream(dev)
+
+    def timed(fn):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        r = fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return r, e0.elapsed_time(e1)
+
+    (F, _), grad_ms = timed(lambda: vg.compute_grads_factored(fxs, model))
+    (_, E), eloc_ms = timed(lambda: vg.evaluate_energy(fxs, model, H))
+    solver = vg.MinSRGB300(record_stages=True)
+    (dp, _, info), sr_ms = timed(lambda: solver.solve(local_o=F, local_energies=E, energy_mean=float(E.mean()),
+                                                      total_samples=fxs.shape[0], n_params=model.n_params,
+                                                      diag_shift=diag_shift, device=dev, run_sr=True))
+    Ns, Nd = F.dense.shape
+    Ng, Nh = F.g.shape[1], F.h.shape[1]
+    st = solver.last_stages or {}
+    fl = {"gram_dense": 2.0 * Ns * Ns * Nd, "gram_head": 2.0 * Ns * Ns * (Ng + Nh) + 2.0 * Ns * Ng * Nh,
+          "cholesky": Ns ** 3 / 3.0}
+    stages = {}
+    for k, ms in st.items():
+        d = {"ms": ms}
+        if k in fl:
+            d["tflops"] = fl[k] / (ms / 1e3) / 1e12
+            d["flop"] = fl[k]
+        stages[k] = d
+    if "gram_dense" in stages:
+        stages["gram_dense"]["frac_of_fp32_nominal"] = stages["gram_dense"]["tflops"] / fp32_peak_tflops
+    if "cholesky" in stages:
+        stages["cholesky"]["frac_of_fp64_nominal"] = stages["cholesky"]["tflops"] / 1.25
+    o_bytes = Ns * (Nd + Ng + Nh) * F.dense.element_size()
+    return {"workload": "8x8 NNBF, %d walkers: per-sample O (FP32, dense %d + Kronecker %d x %d), E_loc, minSR "
+                        "over %d parameters (diag shift %g)" % (Ns, Nd, Ng, Nh, model.n_params, diag_shift),
+            "logpsi_grad_ms": grad_ms, "O_bytes_written": o_bytes,
+            "O_write_gbs": o_bytes / (grad_ms / 1e3) / 1e9, "local_energy_ms": eloc_ms, "minsr_ms": sr_ms,
+            "minsr_stages": stages, "info": info, "dp_norm": float(dp.norm().item()),
+            "peaks": "FP32 nominal %.1f TFLOP/s (152 SM x 128 lanes x 2 x max SM clock), FP64 nominal 1.25 TFLOP/s"
+                     % fp32_peak_tflops}
 
 
 # ---------------------------------------------------------------------------
@@ -474,10 +566,21 @@ def run_gb300(args):
     per_edge = sum(2 + 2 * -(-min(bg, B - g * bg) // 4096) for g in range(G) if g * bg < B)
     gpu_launches = args.steps * (E * per_edge + 2 + 2 * n_chunks + 1)
 
-    ess = ess_compare(model, H, fxs, dev) if not args.no_ess else None
     smax = clocks.get("sm_max_mhz") or 2070.0
-    peps = peps_block(dev, 2, 152 * 128 * 2 * smax * 1e6 / 1e12, cpu=(rank == 0 and not args.no_cpu_baseline)) \
-        if not args.no_peps else None
+    fp32_peak = 152 * 128 * 2 * smax * 1e6 / 1e12
+    sr = None
+    if not args.no_sr:
+        try:
+            sr = sr_block(model, H, fxs, dev, fp32_peak)
+        except Exception as e:   # reported in the line; the headline numbers stand
+            sr = {"error": "%s: %s" % (type(e).__name__, e)}
+    ess = None
+    if not args.no_ess:
+        try:
+            ess = ess_block(dev, B)
+        except Exception as e:
+            ess = {"error": "%s: %s" % (type(e).__name__, e)}
+    peps = peps_block(dev, 2, fp32_peak, cpu=(rank == 0 and not args.no_cpu_baseline)) if not args.no_peps else None
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -494,7 +597,7 @@ def run_gb300(args):
                                            "evaluated_proposals_per_step": n_eval / args.steps}),
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
                 "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": gpu_launches,
-                "ess": ess, "fpeps": peps}
+                "ess": ess, "sr": sr, "fpeps": peps}
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
@@ -526,6 +629,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-ess", action="store_true", help="skip the learned-vs-plain ESS/s comparison")
     ap.add_argument("--no-peps", action="store_true", help="skip the secondary 6x6 fPEPS workload")
+    ap.add_argument("--no-sr", action="store_true", help="skip the O + minSR block at the headline size")
     ap.add_argument("--peps-only", action="store_true",
                     help="run only the fPEPS block (print its JSON object); for profiling")
     ap.add_argument("--peps-walkers", type=int, default=PEPS_B, help="walkers of the fPEPS block (default 8192)")

@@ -92,17 +92,59 @@ class FactoredO:
         return torch.cat([dp_dense[:self.offset], dp_kron.reshape(-1), dp_dense[self.offset:]])
 
 
+class _Stages:
+    """Optional per-stage device times of one solve: CUDA events recorded on
+    the current stream; ``mark(name)`` closes the stage called ``name``."""
+
+    def __init__(self, enabled):
+        self.ev = [("start", self._event())] if enabled else None
+
+    @staticmethod
+    def _event():
+        e = torch.cuda.Event(enable_timing=True)
+        e.record()
+        return e
+
+    def mark(self, name):
+        if self.ev is not None:
+            self.ev.append((name, self._event()))
+
+    def result(self):
+        if self.ev is None:
+            return None
+        self.ev[-1][1].synchronize()
+        out = {}
+        for (_, a), (name, b) in zip(self.ev[:-1], self.ev[1:]):
+            out[name] = out.get(name, 0.0) + a.elapsed_time(b)
+        return out
+
+
 class PreconditionerGB300:
     def solve(self, *, local_o, local_energies, energy_mean, total_samples, n_params, diag_shift, device, run_sr):
         raise NotImplementedError
 
 
 class MinSRGB300(PreconditionerGB300):
-    """Drop-in for MinSRGPU.solve (vmc_torch/GPU/optimizer.py:884-907)."""
+    """Drop-in for MinSRGPU.solve (vmc_torch/GPU/optimizer.py:884-907).
+
+    record_stages=True keeps the device time of each stage of the last solve
+    (centring, Gram blocks, Cholesky, triangular solves, update) in
+    ``last_stages`` (milliseconds, CUDA events on the current stream)."""
+
+    def __init__(self, record_stages=False):
+        self.record_stages = record_stages
+        self.last_stages = None
 
     def solve(self, *, local_o, local_energies, energy_mean, total_samples, n_params, diag_shift, device=None,
               run_sr=True):
         t0 = time.time()
+        self._st = _Stages(self.record_stages and run_sr)
+        try:
+            return self._solve(local_o, local_energies, energy_mean, n_params, diag_shift, device, run_sr, t0)
+        finally:
+            self.last_stages = self._st.result()
+
+    def _solve(self, local_o, local_energies, energy_mean, n_params, diag_shift, device, run_sr, t0):
         dev = torch.device(device) if device is not None else torch.device("cuda")
         E = torch.as_tensor(local_energies, device=dev, dtype=torch.float64).contiguous()
         if isinstance(local_o, FactoredO):
@@ -123,27 +165,32 @@ class MinSRGB300(PreconditionerGB300):
             return g, time.time() - t0, None
         Oc = torch.empty_like(O)
         _lib.call("vmc_sr_center", _lib.ptr(O), code, Ns, Np, O.stride(0), _lib.ptr(Oc), Oc.stride(0), None, s)
+        self._st.mark("center")
 
         def gram(T, shift):
             _lib.call("vmc_sr_gram", _lib.ptr(Oc), code, Ns, Np, Oc.stride(0), _lib.ptr(T), Ns, shift, 0, s)
+            self._st.mark("gram")
 
-        x, info = self._factor_solve(gram, E, float(energy_mean), Ns, float(diag_shift), dev)
+        x, info = self._factor_solve(gram, E, float(energy_mean), Ns, float(diag_shift), dev, self._st)
         dp = torch.empty(Np, dtype=torch.float64, device=dev)
         _lib.call("vmc_sr_update", _lib.ptr(Oc), code, Ns, Np, Oc.stride(0), _lib.ptr(x), _lib.ptr(dp), s)
+        self._st.mark("update")
         return dp, time.time() - t0, info
 
     # -- shared: Gram -> FP64 Cholesky -> solve (reference fallbacks on failure) --
     @staticmethod
-    def _factor_solve(build_gram, E, Ebar, Ns, shift, dev):
+    def _factor_solve(build_gram, E, Ebar, Ns, shift, dev, stages):
         s = _lib.stream_of(dev)
         T = torch.empty((Ns, Ns), dtype=torch.float64, device=dev)
         build_gram(T, shift)
         flag = torch.zeros(1, dtype=torch.int32, device=dev)
         _lib.call("vmc_sr_cholesky", _lib.ptr(T), Ns, Ns, _lib.ptr(flag), s)
+        stages.mark("cholesky")
         x = torch.empty(Ns, dtype=torch.float64, device=dev)
         _lib.call("vmc_sr_rhs", _lib.ptr(E), Ns, Ebar, _lib.ptr(x), s)
         if int(flag.item()) == 0:
             _lib.call("vmc_sr_cholesky_solve", _lib.ptr(T), Ns, Ns, _lib.ptr(x), s)
+            stages.mark("solve")
             return x, 0
         # the factorisation overwrote T: rebuild it, then solve as the reference does
         build_gram(T, shift)
@@ -167,6 +214,7 @@ class MinSRGB300(PreconditionerGB300):
         mu = torch.empty((Ng, Nh), dtype=torch.float64, device=dev)
         _lib.call("vmc_gemm", 1, 0, Ng, Nh, Ns, 1.0 / Ns, _lib.ptr(G), G.stride(0), _lib.ptr(H), H.stride(0), None,
                   code, 0.0, _lib.ptr(mu), Nh, None, 0, 0, s)
+        self._st.mark("gram_head")
         if not run_sr:
             g = torch.empty(Nd, dtype=torch.float64, device=dev)
             _lib.call("vmc_energy_gradient", _lib.ptr(Od), code, Ns, Nd, Od.stride(0), _lib.ptr(E), Ebar, _lib.ptr(g), s)
@@ -178,6 +226,7 @@ class MinSRGB300(PreconditionerGB300):
             return F.assemble(g, gk), time.time() - t0, None
         Oc = torch.empty_like(Od)
         _lib.call("vmc_sr_center", _lib.ptr(Od), code, Ns, Nd, Od.stride(0), _lib.ptr(Oc), Oc.stride(0), None, s)
+        self._st.mark("center")
         HH = torch.empty((Ns, Ns), dtype=torch.float64, device=dev)
         _lib.call("vmc_gemm", 0, 1, Ns, Ns, Nh, 1.0, _lib.ptr(H), H.stride(0), _lib.ptr(H), H.stride(0), None, code,
                   0.0, _lib.ptr(HH), Ns, None, 0, 1, s)
@@ -187,15 +236,18 @@ class MinSRGB300(PreconditionerGB300):
                   _lib.ptr(P), Nh, None, 0, 0, s)
         mu_sq = float((mu * mu).sum().item())
         vwork = torch.empty(Ns, dtype=torch.float64, device=dev)
+        self._st.mark("gram_head")
 
         def gram(T, sh):
             _lib.call("vmc_sr_gram", _lib.ptr(Oc), code, Ns, Nd, Oc.stride(0), _lib.ptr(T), Ns, sh, 0, s)
+            self._st.mark("gram_dense")
             _lib.call("vmc_gemm", 0, 1, Ns, Ns, Ng, 1.0 / Ns, _lib.ptr(G), G.stride(0), _lib.ptr(G), G.stride(0),
                       None, code, 1.0, _lib.ptr(T), Ns, _lib.ptr(HH), Ns, 1, s)
             _lib.call("vmc_sr_kron_correction", Ns, _lib.ptr(T), Ns, _lib.ptr(P), Nh, _lib.ptr(H), code, H.stride(0),
                       Nh, mu_sq, 1.0 / Ns, _lib.ptr(vwork), s)
+            self._st.mark("gram_head")
 
-        x, info = self._factor_solve(gram, E, Ebar, Ns, shift, dev)
+        x, info = self._factor_solve(gram, E, Ebar, Ns, shift, dev, self._st)
         dp_d = torch.empty(Nd, dtype=torch.float64, device=dev)
         _lib.call("vmc_sr_update", _lib.ptr(Oc), code, Ns, Nd, Oc.stride(0), _lib.ptr(x), _lib.ptr(dp_d), s)
         rs = Ns ** 0.5
@@ -203,6 +255,7 @@ class MinSRGB300(PreconditionerGB300):
         xc = x.to(G.dtype).contiguous()
         _lib.call("vmc_gemm", 1, 0, Ng, Nh, Ns, 1.0 / rs, _lib.ptr(G), G.stride(0), _lib.ptr(H), H.stride(0),
                   _lib.ptr(xc), code, 1.0, _lib.ptr(dp_k), Nh, None, 0, 0, s)
+        self._st.mark("update")
         return F.assemble(dp_d, dp_k), time.time() - t0, info
 
 
