@@ -14,9 +14,13 @@ from pinned host memory before each step and the configurations plus
 log-amplitudes copied back after it.  L2 is flushed (256 MB write) between
 timed steps.
 
---impl reference times the reference algorithm on the host CPU: the CPU port
-of the reference's batched sampler (oracle/sampler.py with the FP64 NNBF
-amplitude of oracle/models.py), on a bounded sample of walkers per step.
+--impl reference times the reference's own implementation on the host CPU:
+its batched sampler (MetropolisExchangeSpinfulSamplerGPU) and NNBF_GPU model,
+imported from its pip install in baseline/_ref under the import shims of its
+absent tensor-network / MPI dependencies, one single-thread process per core
+with 16 chains each (the reference's MPI ranks run independent chains too).
+Where that install is absent, the CPU port of the same sampler
+(oracle/sampler.py with the FP64 NNBF amplitude of oracle/models.py) stands in.
 """
 import argparse
 import json
@@ -147,25 +151,97 @@ def cpu_port_rate(n_walkers=48, n_sweeps=1, seed=0):
         n_walkers, S, E)
 
 
+REF_ROOT = os.path.join(ROOT, "baseline", "_ref")
+_ref = {}
+
+
+def _ref_init(root, n_walkers, seed):
+    """Worker set-up: the reference's own batched sampler and NNBF_GPU model
+    (imported from its pip install under the import shims of its absent TN /
+    MPI dependencies), one CPU thread, ``n_walkers`` seeded chains."""
+    os.environ["OMP_NUM_THREADS"] = "1"
+    import torch
+    torch.set_num_threads(1)
+    from oracle import lattice, models, refshim
+    ht = refshim.load("vmc_torch.hamiltonian_torch", root)
+    smp = refshim.load("vmc_torch.GPU.sampler", root)
+    nn = refshim.load("vmc_torch.GPU.models.NNBF", root)
+    H = ht.spinful_Fermi_Hubbard_square_lattice_torch(LX, LY, 1.0, 8.0, NUP + NDN, n_fermions_per_spin=(NUP, NDN))
+    model = nn.NNBF_GPU(LX * LY, NUP + NDN, hidden_dim=HID, n_layers=2, activation="gelu", bf_scale=BF_SCALE)
+    with torch.no_grad():
+        for p, v in zip(model.params, models.nnbf_init(LX * LY, NUP + NDN, HID, 2, seed=0)):
+            p.copy_(torch.as_tensor(v))
+    fx = torch.as_tensor(lattice.random_initial_configs(n_walkers, LX * LY, NUP, NDN, seed=seed + os.getpid()))
+    _ref.update(H=H, model=model, sampler=smp.MetropolisExchangeSpinfulSamplerGPU(), fx=fx, torch=torch)
+
+
+def _ref_sweep(_):
+    """One reference sweep (112 edges) of this worker's chains: (walker-steps, seconds)."""
+    torch = _ref["torch"]
+    t0 = time.perf_counter()
+    with torch.inference_mode():
+        _ref["fx"], _ = _ref["sampler"].step(_ref["fx"], _ref["model"], _ref["H"].graph)
+    n_edges = 2 * LX * LY - LX - LY   # nearest-neighbour edges of the open LX x LY lattice: one sweep
+    return _ref["fx"].shape[0] * n_edges, time.perf_counter() - t0
+
+
+def reference_pool(n_procs, n_walkers):
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    return ctx.Pool(n_procs, initializer=_ref_init, initargs=(REF_ROOT, n_walkers, 17))
+
+
+def reference_rate(pool, n_procs):
+    """One timed round: every worker runs one sweep of its own chains at once
+    (independent chains, no communication, as the reference's MPI ranks);
+    throughput = all walker-steps over the slowest worker's time."""
+    res = pool.map(_ref_sweep, range(n_procs))
+    return sum(r[0] for r in res) / max(r[1] for r in res)
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
     world = int(os.environ.get("WORLD_SIZE", "1"))
     cores = os.cpu_count()
-    for _ in range(args.warmup):
-        cpu_port_rate(n_walkers=16, n_sweeps=1)
-    rates, tot = [], 0.0
-    for k in range(args.steps):
-        r, dt, sample = cpu_port_rate(n_walkers=48, n_sweeps=1, seed=k)
-        rates.append(r)
-        tot += dt
-    value = float(np.mean(rates))
+    if os.path.isdir(os.path.join(REF_ROOT, "vmc_torch")):
+        # the reference's own batched sampler + NNBF_GPU on every host core:
+        # one single-thread process per core, 16 chains each
+        nw = 16
+        pool = reference_pool(cores, nw)
+        try:
+            for _ in range(args.warmup):
+                reference_rate(pool, cores)
+            rates = []
+            t0 = time.perf_counter()
+            for _ in range(args.steps):
+                rates.append(reference_rate(pool, cores))
+            tot = time.perf_counter() - t0
+        finally:
+            pool.close()
+            pool.join()
+        value = float(np.mean(rates))
+        kind = "reference"
+        sample = ("the reference's MetropolisExchangeSpinfulSamplerGPU + NNBF_GPU(2x256 GELU) on the host CPU: "
+                  "%d single-thread processes x %d chains x 1 sweep (112 edges) per step" % (cores, nw))
+        dtype = "f64 (reference defaults)"
+    else:
+        for _ in range(args.warmup):
+            cpu_port_rate(n_walkers=16, n_sweeps=1)
+        rates, tot = [], 0.0
+        for k in range(args.steps):
+            r, dt, sample = cpu_port_rate(n_walkers=48, n_sweeps=1, seed=k)
+            rates.append(r)
+            tot += dt
+        value = float(np.mean(rates))
+        kind = "port"
+        dtype = "f64"
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "scaling": "weak", "vs_baseline": None, "dtype": dtype, "data": "synthetic (seeded)",
             "config": workload_config({"sample": sample}), "impl": "reference",
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -584,9 +660,24 @@ def run_gb300(args):
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        r, dt, sample = cpu_port_rate(n_walkers=48, n_sweeps=1)
-        cpu = {"value": r, "unit": UNIT, "cores": os.cpu_count(), "kind": "port", "sample": sample,
-               "seconds": dt}
+        cores = os.cpu_count()
+        if os.path.isdir(os.path.join(REF_ROOT, "vmc_torch")):
+            pool = reference_pool(cores, 16)
+            try:
+                t0 = time.perf_counter()
+                reference_rate(pool, cores)   # warm-up round
+                rates = [reference_rate(pool, cores) for _ in range(3)]
+                dt = time.perf_counter() - t0
+            finally:
+                pool.close()
+                pool.join()
+            cpu = {"value": float(np.mean(rates)), "unit": UNIT, "cores": cores, "kind": "reference",
+                   "sample": "the reference's MetropolisExchangeSpinfulSamplerGPU + NNBF_GPU(2x256 GELU) on the "
+                             "host CPU: %d single-thread processes x 16 chains, 3 timed sweeps" % cores,
+                   "seconds": dt}
+        else:
+            r, dt, sample = cpu_port_rate(n_walkers=48, n_sweeps=1)
+            cpu = {"value": r, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample, "seconds": dt}
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,

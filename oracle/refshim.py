@@ -40,17 +40,31 @@ class _StubFinder(importlib.abc.MetaPathFinder, importlib.abc.Loader):
 
 
 _installed = False
+# optional packages the reference imports at module level: stubbed only where
+# they are not installed (the GPU host ships without them)
+_OPTIONAL = ("tqdm",)
 
 
-def install():
-    """Install the shims and put the reference on sys.path (idempotent)."""
+def install(root=None):
+    """Install the shims and put the reference on sys.path (idempotent).
+    root: the directory holding the ``vmc_torch`` package (a checkout, or a
+    pip --target install); default VMC_REFERENCE_ROOT."""
     global _installed
     if _installed:
         return
-    if not REFERENCE_ROOT or not os.path.isdir(os.path.join(REFERENCE_ROOT, "vmc_torch")):
-        raise RuntimeError("set VMC_REFERENCE_ROOT to a checkout of sjdu10/vmc_torch (the directory holding "
-                           "the vmc_torch package) to import the reference")
+    root = root or REFERENCE_ROOT
+    if not root or not os.path.isdir(os.path.join(root, "vmc_torch")):
+        raise RuntimeError("give the directory holding the reference's vmc_torch package (argument or "
+                           "VMC_REFERENCE_ROOT) to import the reference")
     import torch
+    global _STUB
+    missing = []
+    for name in _OPTIONAL:
+        try:
+            importlib.import_module(name)
+        except ImportError:
+            missing.append(name)
+    _STUB = _STUB + tuple(missing)
 
     sys.meta_path.insert(0, _StubFinder())
     ar = types.ModuleType("autoray")
@@ -65,7 +79,7 @@ def install():
 
     ar.do = do
     sys.modules["autoray"] = ar
-    sys.path.insert(0, REFERENCE_ROOT)
+    sys.path.insert(0, root)
     import quimb.tensor as qtn  # the MagicMock stub
     from .lattice import square_edges
 
@@ -80,6 +94,6 @@ def install():
     _installed = True
 
 
-def load(modname):
-    install()
+def load(modname, root=None):
+    install(root)
     return importlib.import_module(modname)

@@ -139,7 +139,10 @@ def compute_grads_factored(fxs, model, use_log_amp=True, **kwargs):
     form (``optimizer.FactoredO``), for sample-space SR at scale.  Always in log
     mode: returns (FactoredO, (signs, log_abs))."""
     from .optimizer import FactoredO
-    with torch.inference_mode():
+    # no_grad, not inference mode: the returned tensors are ordinary tensors
+    # that the caller may update in place (the reference's driver divides O
+    # by the amplitudes in place, vmc_torch/GPU/VMC.py:453)
+    with torch.no_grad():
         st = model.bind_state(fxs)
         Od, g, h = model.logpsi_grad_factored(st)
         model.check_status(st, wait=True)
@@ -153,7 +156,11 @@ def compute_grads_factored(fxs, model, use_log_amp=True, **kwargs):
 
 def compute_grads_gpu(fxs, model, batch_size=None, verbose=False, offload_to_cpu=False, use_log_amp=False,
                       vectorize=True, vmap_grad=True, bMPS_params_x=None, **kwargs):
-    with torch.inference_mode():
+    # no_grad, not inference mode: O, the amplitudes and the log-amplitudes are
+    # returned as ordinary tensors the caller may update in place (the
+    # reference's driver divides O by the amplitudes in place,
+    # vmc_torch/GPU/VMC.py:453)
+    with torch.no_grad():
         st = model.bind_state(fxs)
         B, Np = st.B, model.n_params
         bs = int(batch_size) if batch_size else B

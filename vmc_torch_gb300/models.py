@@ -100,9 +100,12 @@ class WavefunctionModel_GB300(nn.Module):
     def _new_state(self, B, device):
         return WalkerState(B, self.n_sites, device)
 
+    @torch.inference_mode()
     def bind_state(self, fxs):
         """Return the walker state for ``fxs``, re-packing and re-evaluating the
-        amplitudes when fxs or the parameters changed since the last use."""
+        amplitudes when fxs or the parameters changed since the last use.  The
+        state's tensors are inference tensors, updated in place by the kernels;
+        values handed back to callers are copies."""
         _lib.require_cuda(fxs, "fxs")
         if fxs.dim() != 2 or fxs.shape[1] != self.n_sites:
             raise ValueError("fxs must be (B, %d) int64" % self.n_sites)
@@ -120,6 +123,7 @@ class WavefunctionModel_GB300(nn.Module):
         st.param_key = pk
         return st
 
+    @torch.inference_mode()
     def _eval_state(self, x):
         """A fresh state for arbitrary configs (not bound)."""
         st = self._new_state(x.shape[0], x.device)
