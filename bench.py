@@ -347,8 +347,8 @@ def peps_block(dev, steps, fp32_peak_tflops, cpu=True, env_reuse=True):
 
 
 # ---------------------------------------------------------------------------
-def ess_block(dev, n_walkers, samples=160, discard=16, moves=28, sr_steps=20, pre_walkers=4096, every=10, epochs=2,
-              lr=0.02):
+def ess_block(dev, n_walkers, samples=192, discard=32, moves=14, sr_steps=20, pre_walkers=4096, every=10, epochs=1,
+              lr=0.02, burn=40):
     """ESS/s of E_loc for plain exchange/hop Metropolis (one 112-edge sweep per
     sample) vs the learned proposal (``moves`` MH moves per sample) on the 8x8
     backflow model after ``sr_steps`` SR steps (not at random init).
@@ -362,7 +362,10 @@ def ess_block(dev, n_walkers, samples=160, discard=16, moves=28, sr_steps=20, pr
     ESS/s is reported three ways: (a) sampler device time only; (b) with the
     proposal's training charged as on the schedule, one session per ``every``
     samples (one sample per chain per SR step); (c) with the local-energy
-    device time of every sample added to both samplers; and (b)+(c)."""
+    device time of every sample added to both samplers; and (b)+(c).  The
+    measurement walkers are first equilibrated by ``burn`` plain sweeps at the
+    final parameters; the mean energies of the first and second halves of the
+    used samples show any remaining drift."""
     import torch
     import vmc_torch_gb300 as vg
     from vmc_torch_gb300.proposal import LearnedProposal, LearnedSamplerGB300, OnlineProposalTraining
@@ -388,7 +391,7 @@ def ess_block(dev, n_walkers, samples=160, discard=16, moves=28, sr_steps=20, pr
     t_train = hook.train_seconds / max(hook.sessions, 1)
 
     x = vg.init_walkers(n_walkers, LX * LY, NUP, NDN, seed=78, device=dev)
-    plain.burn_in(x, model, graph, 8)
+    plain.burn_in(x, model, graph, burn)
     learned = LearnedSamplerGB300(prop, moves_per_step=moves)
 
     def run(sampler, x0):
@@ -407,6 +410,8 @@ def ess_block(dev, n_walkers, samples=160, discard=16, moves=28, sr_steps=20, pr
         E = torch.stack(Es[discard:]).t().contiguous()
         tau = tau_int(E)
         nb, used = E.shape
+        half = used // 2
+        drift = [float(E[:, :half].mean().item()) / (LX * LY), float(E[:, half:].mean().item()) / (LX * LY)]
         ess = nb * used / tau
         f = used / samples
         return {"tau_int_samples": tau, "ess": ess, "sampler_s": ts, "eloc_s": te,
@@ -414,7 +419,7 @@ def ess_block(dev, n_walkers, samples=160, discard=16, moves=28, sr_steps=20, pr
                 "ess_per_s": ess / (ts * f), "ess_per_s_with_eloc": ess / ((ts + te) * f),
                 "energy_per_site": float(E.mean().item()) / (LX * LY),
                 "stderr_per_site": float(E.std().item()) / (LX * LY) * (tau / (nb * used)) ** 0.5,
-                "split_rhat": split_rhat(E)}
+                "split_rhat": split_rhat(E), "energy_per_site_halves": drift}
 
     rp = run(plain, x)
     rl = run(learned, x)
@@ -438,6 +443,7 @@ def ess_block(dev, n_walkers, samples=160, discard=16, moves=28, sr_steps=20, pr
             "abs_dE_per_site": dE, "matched_energy_1e-3": dE < 1e-3,
             "dE_sigma": dE / (rp["stderr_per_site"] ** 2 + rl["stderr_per_site"] ** 2) ** 0.5,
             "walkers": n_walkers, "samples_per_chain": samples, "discarded_per_chain": discard,
+            "burn_in_sweeps": burn,
             "learned_moves_per_sample": moves, "learned_acceptance": acc,
             "wavefunction": {"sr_steps_before_measuring": sr_steps, "sr_walkers": pre_walkers, "lr": lr,
                              "diag_shift": 1e-3, "energy_per_site_first_last": [hist[0], hist[-1]],

@@ -91,6 +91,38 @@ def test_learned_sampler_is_stationary_on_4x2():
     assert tv < 1.5 * tvc + 0.005
 
 
+def test_fused_mixed_step_matches_generic_path():
+    """The mixed NNBF model's fused learned-MH step (proposal evaluation, LU
+    and Metropolis-Hastings accept in one call) makes the same decisions as
+    the model-agnostic path whose stationarity the 4x2 test shows: same
+    proposals (two proposal objects with one seed and one set of weights),
+    same amplitudes, so the chains coincide up to acceptance tests within the
+    FP32 rounding of the fused ratio."""
+    Lx, Ly, nup, B = 6, 6, 16, 2048
+    N = Lx * Ly
+    H = vg.spinful_Fermi_Hubbard_square_lattice_torch(Lx, Ly, 1.0, 8.0, 2 * nup, n_fermions_per_spin=(nup, nup))
+    model = _nnbf_6x6(21)
+    props = []
+    for _ in range(2):
+        p = LearnedProposal(N, H.edges_on(DEV), device=DEV, seed=23)
+        with torch.no_grad():
+            p.params.mul_(2.0)
+        p.t += 1
+        props.append(p)
+    x0 = vg.init_walkers(B, N, nup, nup, seed=24, device=DEV)
+    xf, xg = x0.clone(), x0.clone()
+    _, (sf, lf) = LearnedSamplerGB300(props[0], moves_per_step=12).step(xf, model, H.graph, use_log_amp=True)
+    _, (sg, lg) = LearnedSamplerGB300(props[1], moves_per_step=12, fused=False).step(xg, model, H.graph,
+                                                                                     use_log_amp=True)
+    same = (xf == xg).all(1)
+    print("fused vs generic learned MH: %d/%d chains identical, accepted %d / %d"
+          % (int(same.sum()), B, int(props[0].kstats[4:].sum()), int(props[1].kstats[4:].sum())))
+    assert not torch.equal(xf, x0)
+    assert same.double().mean().item() > 0.995
+    assert torch.equal(props[0].kstats, props[1].kstats) or same.double().mean().item() > 0.995
+    assert (lf[same] - lg[same]).abs().max().item() < 1e-2
+
+
 def _nnbf_6x6(seed=7):
     g = torch.Generator().manual_seed(seed)
     return vg.NNBF_GB300(36, 32, precision="mixed", generator=g).to(DEV)

@@ -203,9 +203,12 @@ class LearnedSamplerGB300(SamplerGB300):
     and the walkers move by the model-agnostic vmc_accept_mh, after which the
     model's per-walker state is rebuilt for the new configurations."""
 
-    def __init__(self, proposal, moves_per_step=112):
+    def __init__(self, proposal, moves_per_step=112, fused=None):
+        """fused: None picks the fused step where the model has one; False
+        forces the model-agnostic path (evaluation + vmc_accept_mh)."""
         self.proposal = proposal
         self.moves_per_step = moves_per_step
+        self.fused = fused
         self._st = []
 
     def _streams(self, n, device):
@@ -215,8 +218,9 @@ class LearnedSamplerGB300(SamplerGB300):
 
     GROUP = 4096   # walkers per group when the batch is split over streams
 
-    @staticmethod
-    def _native(model):
+    def _native(self, model):
+        if self.fused is False:
+            return False
         return getattr(model, "precision", None) == "mixed" and hasattr(model, "mh_step")
 
     def _generic_moves(self, st, model):
