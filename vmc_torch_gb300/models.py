@@ -296,13 +296,19 @@ class SlaterDeterminant_GB300(WavefunctionModel_GB300):
             for a in (rm, rb, ra):
                 if tuple(a.shape) != (n_sweeps, E, st.B) or not a.is_cuda or not a.is_contiguous():
                     raise ValueError("replay buffers must be contiguous CUDA tensors of shape (n_sweeps, E, B)")
-        _lib.call("vmc_slater_sweep", _lib.ptr(M), self.n_orbitals, self.n_fermions, _lib.ptr(st.occ), st.B,
-                  self.n_sites, _lib.ptr(edges), edges.shape[0], int(n_sweeps), float(hopping_rate),
-                  int(seed) & ((1 << 64) - 1), int(sweep_offset), _lib.ptr(rm), _lib.ptr(rb), _lib.ptr(ra),
-                  _lib.ptr(st.extra["G"]), _lib.ptr(st.extra["slot"]), _lib.ptr(st.sign), _lib.ptr(st.logabs),
-                  _lib.ptr(st.n_acc), _lib.stream_of(st.device))
-        if self.refresh_every:
-            self._refresh(st, threshold=self.refresh_every)
+        # one launch per sweep, so that the FP64 re-inversion of every walker
+        # with refresh_every or more accepted moves since its last one (which
+        # resets the Sherman-Morrison drift) runs between sweeps, also in a
+        # long burn-in
+        for k in range(int(n_sweeps)):
+            part = (None, None, None) if replay is None else tuple(a[k:k + 1] for a in (rm, rb, ra))
+            _lib.call("vmc_slater_sweep", _lib.ptr(M), self.n_orbitals, self.n_fermions, _lib.ptr(st.occ), st.B,
+                      self.n_sites, _lib.ptr(edges), edges.shape[0], 1, float(hopping_rate),
+                      int(seed) & ((1 << 64) - 1), int(sweep_offset) + k, _lib.ptr(part[0]), _lib.ptr(part[1]),
+                      _lib.ptr(part[2]), _lib.ptr(st.extra["G"]), _lib.ptr(st.extra["slot"]), _lib.ptr(st.sign),
+                      _lib.ptr(st.logabs), _lib.ptr(st.n_acc), _lib.stream_of(st.device))
+            if self.refresh_every:
+                self._refresh(st, threshold=self.refresh_every)
 
     def local_energy(self, st, H):
         M = self._M(st.device)
