@@ -110,6 +110,14 @@ int vmc_slater_logpsi_grad(const double* G, const uint8_t* slot_orb, int64_t B, 
  * and VMC_ERR_ARGS if a configuration evaluated from scratch has an occupation
  * bit at or above n_sites or other than nf electrons (its result is then
  * meaningless; bits above n_sites are ignored, never used as indices).
+ * Streams: work is enqueued on `stream`; for R > 4096 (mixed precision) the
+ * call may fork part of it onto library-owned streams (one high-priority stream
+ * for the next chunk's backflow GEMM, up to four for independent walker groups),
+ * created once per device and shared by all callers, and joins them back into
+ * `stream` by events before it returns, on error paths too.  Calls issued
+ * concurrently from several host threads therefore share those streams.
+ * Environment: VMC_GB300_SERIAL_CHUNKS=1 / VMC_GB300_SWEEP_LANES=1 keep all
+ * work on `stream`.
  * Amplitude results: a singular orbital matrix gives sign 0 and logabs -inf; a
  * NaN or Inf entry (non-finite parameters) gives NaN for both, as the
  * reference's NaN amplitude.  Metropolis tests never accept a NaN ratio; from a
@@ -263,6 +271,21 @@ int vmc_sr_center(const void* O, int dtype, int64_t Ns, int64_t Np, int64_t ldo,
 int vmc_sr_gram(const void* Oc, int dtype, int64_t Ns, int64_t Np, int64_t ldc, double* T, int64_t ldt,
                 double diag_shift, int accumulate, void* stream);
 int vmc_sr_cholesky(double* T, int64_t n, int64_t ldt, int* d_info, void* stream);
+/* Tensor-core Gram for FP32 inputs (no reference counterpart as an operator:
+ * the reference forms lpg_scaled @ lpg_scaled.T in FP64, vmc_torch/GPU/optimizer.py:551-553).
+ * vmc_split_bf16x3: X (rows, K, ld ldx) FP32 -> three BF16 planes hi, mid, lo
+ *   (x = hi + mid + lo to 2^-24), each (rows_pad, kp) row-major, rows_pad a
+ *   multiple of 128 >= rows, kp a multiple of 64 >= K, padding zeroed; planes
+ *   holds 3 * rows_pad * kp bf16.
+ * vmc_sr_gram_tc: T (ns, ns, FP64, ld ldt) = [T +] alpha (X X^T) o D [+ shift I]
+ *   with D (nullable, ld ldt) elementwise and `accumulate` selecting "+=";
+ *   six BF16 products per element pair on tcgen05 with FP32 accumulation,
+ *   drained into FP64 every 2048 columns; the full symmetric T is written.
+ *   d_err (device int) receives VMC_ERR_TIMEOUT if a bounded wait gave up. */
+int vmc_split_bf16x3(const float* X, int64_t rows, int64_t K, int64_t ldx, void* planes, int64_t rows_pad,
+                     int64_t kp, void* stream);
+int vmc_sr_gram_tc(const void* planes, int64_t ns, int64_t rows_pad, int64_t kp, double alpha, double* T,
+                   int64_t ldt, const double* D, double diag_shift, int accumulate, int* d_err, void* stream);
 int vmc_sr_cholesky_solve(const double* L, int64_t n, int64_t ldt, double* b, void* stream);
 int vmc_sr_rhs(const double* E, int64_t Ns, double Ebar, double* b, void* stream);
 int vmc_sr_update(const void* Oc, int dtype, int64_t Ns, int64_t Np, int64_t ldc, const double* x, double* dp,

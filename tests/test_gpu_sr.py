@@ -66,3 +66,54 @@ def test_factored_minsr_mixed_precision_vs_fp64():
     r = rel(dp32.cpu().numpy(), dp64.cpu().numpy())
     print("mixed factored minSR direction rel err %.2e" % r)
     assert info == 0 and r < 2e-3
+
+
+@pytest.mark.parametrize("Ns,K", [(700, 3000), (256, 115200 // 16)])
+def test_tensor_core_gram_matches_compensated_fp32(Ns, K):
+    """vmc_sr_gram_tc (BF16 three-way split, six products on tcgen05, FP32
+    partial sums over 2048 columns drained into FP64) against the CUDA-core
+    Gram with double-float accumulation (FP64-level) on the same FP32 matrix:
+    entries within 1e-5 of the largest diagonal entry (FP32 rounding of the
+    partial sums of up to 768 tensor-core steps per chunk), also with the
+    elementwise factor D and accumulation used by the Kronecker head."""
+    from vmc_torch_gb300 import _lib
+    g = torch.Generator().manual_seed(Ns)
+    X = (torch.randn(Ns, K, generator=g) * 0.3 + 0.05).float().to(DEV)
+    s = _lib.stream_of(DEV)
+    T_ref = torch.empty((Ns, Ns), dtype=torch.float64, device=DEV)
+    _lib.call("vmc_sr_gram", _lib.ptr(X), 1, Ns, K, X.stride(0), _lib.ptr(T_ref), Ns, 1e-3, 0, s)
+    solver = vg.MinSRGB300()
+    T = torch.full((Ns, Ns), 7.0, dtype=torch.float64, device=DEV)
+    solver._tc_gram(X, T, 1.0, None, 1e-3, 0, DEV)
+    solver._check_tc()
+    scale = T_ref.diagonal().abs().max().item()
+    err = (T - T_ref).abs().max().item() / scale
+    print("tensor-core Gram (%d x %d): max rel err %.2e" % (Ns, K, err))
+    assert err < 1e-5
+    assert torch.equal(T, T.t())
+    # head form: T += alpha (X X^T) o D
+    D = torch.rand((Ns, Ns), generator=g, dtype=torch.float64).to(DEV)
+    D = D + D.t()
+    T2 = T.clone()
+    solver._tc_gram(X, T2, 0.5, D, 0.0, 1, DEV)
+    ref2 = T_ref + 0.5 * (T_ref - 1e-3 * torch.eye(Ns, dtype=torch.float64, device=DEV)) * D
+    err2 = (T2 - ref2).abs().max().item() / scale
+    assert err2 < 2e-5
+
+
+def test_minsr_tensor_gram_vs_cuda_gram_mixed():
+    """The factored mixed minSR direction with the tensor-core Gram equals the
+    one with the compensated CUDA-core Gram to 1e-4 and FP64 to 2e-3."""
+    m64, X, E = setup("fp64", N=36, nf=32)
+    Ns = X.shape[0]
+    kw = dict(local_energies=E, energy_mean=float(E.mean()), total_samples=Ns, n_params=m64.n_params,
+              diag_shift=1e-3, device=DEV, run_sr=True)
+    F64, _ = vg.compute_grads_factored(X, m64)
+    dp64, _, _ = vg.MinSRGB300().solve(local_o=F64, **kw)
+    m32, _, _ = setup("mixed", N=36, nf=32)
+    F32, _ = vg.compute_grads_factored(X, m32)
+    dpt, _, it = vg.MinSRGB300(gram="tensor").solve(local_o=F32, **kw)
+    dpc, _, ic = vg.MinSRGB300(gram="cuda").solve(local_o=F32, **kw)
+    a, b, c = dpt.cpu().numpy(), dpc.cpu().numpy(), dp64.cpu().numpy()
+    print("minSR tensor vs cuda Gram %.2e, tensor vs FP64 %.2e" % (rel(a, b), rel(a, c)))
+    assert it == ic == 0 and rel(a, b) < 1e-4 and rel(a, c) < 2e-3

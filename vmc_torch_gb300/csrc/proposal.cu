@@ -546,14 +546,17 @@ bool tmap(CUtensorMap* m, const void* base, uint64_t rows, uint64_t cols, uint32
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-bool g_attr = false;
+// kernel attributes are per device: set on each device the first time it is current
+bool g_attr[64] = {};
 
 int gemm_bf16(int epi, const __nv_bfloat16* A, int64_t M, int K, const __nv_bfloat16* Bw, int N, const float* bias,
               void* out, int ldo, int* err, cudaStream_t st) {
-  if (!g_attr) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return VMC_ERR_CUDA;
+  if (!g_attr[dev]) {
     cudaFuncSetAttribute(k_gemm_kloop<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, GSMEM);
     cudaFuncSetAttribute(k_gemm_kloop<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, GSMEM);
-    g_attr = true;
+    g_attr[dev] = true;
   }
   if (K % 64 != 0 || N % TN != 0) return VMC_ERR_ARGS;
   CUtensorMap ta, tb;

@@ -131,9 +131,34 @@ class MinSRGB300(PreconditionerGB300):
     (centring, Gram blocks, Cholesky, triangular solves, update) in
     ``last_stages`` (milliseconds, CUDA events on the current stream)."""
 
-    def __init__(self, record_stages=False):
+    def __init__(self, record_stages=False, gram="tensor"):
+        """gram: "tensor" forms the Gram blocks of FP32 O on the tensor cores
+        (vmc_sr_gram_tc: BF16 three-way split, six products, FP32 partial sums
+        drained into FP64); "cuda" keeps them on the CUDA cores with
+        compensated FP32 accumulation.  FP64 O always uses FP64 arithmetic."""
+        if gram not in ("tensor", "cuda"):
+            raise ValueError("gram must be 'tensor' or 'cuda'")
         self.record_stages = record_stages
         self.last_stages = None
+        self.gram = gram
+
+    def _tc_gram(self, X, T, alpha, D, shift, accumulate, dev):
+        """T [+]= alpha (X X^T) o D [+ shift I] on the tensor cores, X FP32 (Ns, K)."""
+        s = _lib.stream_of(dev)
+        Ns, K = X.shape
+        rp, kp = -(-Ns // 128) * 128, -(-K // 64) * 64
+        planes = torch.empty(3 * rp * kp, dtype=torch.bfloat16, device=dev)
+        _lib.call("vmc_split_bf16x3", _lib.ptr(X), Ns, K, X.stride(0), _lib.ptr(planes), rp, kp, s)
+        err = torch.zeros(1, dtype=torch.int32, device=dev)
+        _lib.call("vmc_sr_gram_tc", _lib.ptr(planes), Ns, rp, kp, float(alpha), _lib.ptr(T), T.stride(0),
+                  _lib.ptr(D), float(shift), int(accumulate), _lib.ptr(err), s)
+        self._tc_err = err
+        del planes
+
+    def _check_tc(self):
+        err = getattr(self, "_tc_err", None)
+        if err is not None and int(err.item()) != 0:
+            raise ValueError("vmc_sr_gram_tc: %s" % _lib.message(int(err.item())))
 
     def solve(self, *, local_o, local_energies, energy_mean, total_samples, n_params, diag_shift, device=None,
               run_sr=True):
@@ -168,9 +193,13 @@ class MinSRGB300(PreconditionerGB300):
         self._st.mark("center")
 
         def gram(T, shift):
-            _lib.call("vmc_sr_gram", _lib.ptr(Oc), code, Ns, Np, Oc.stride(0), _lib.ptr(T), Ns, shift, 0, s)
+            if code == 1 and self.gram == "tensor":
+                self._tc_gram(Oc, T, 1.0, None, shift, 0, dev)
+            else:
+                _lib.call("vmc_sr_gram", _lib.ptr(Oc), code, Ns, Np, Oc.stride(0), _lib.ptr(T), Ns, shift, 0, s)
             self._st.mark("gram")
 
+        gram.check = self._check_tc
         x, info = self._factor_solve(gram, E, float(energy_mean), Ns, float(diag_shift), dev, self._st)
         dp = torch.empty(Np, dtype=torch.float64, device=dev)
         _lib.call("vmc_sr_update", _lib.ptr(Oc), code, Ns, Np, Oc.stride(0), _lib.ptr(x), _lib.ptr(dp), s)
@@ -186,6 +215,9 @@ class MinSRGB300(PreconditionerGB300):
         flag = torch.zeros(1, dtype=torch.int32, device=dev)
         _lib.call("vmc_sr_cholesky", _lib.ptr(T), Ns, Ns, _lib.ptr(flag), s)
         stages.mark("cholesky")
+        check = getattr(build_gram, "check", None)
+        if check is not None:
+            check()
         x = torch.empty(Ns, dtype=torch.float64, device=dev)
         _lib.call("vmc_sr_rhs", _lib.ptr(E), Ns, Ebar, _lib.ptr(x), s)
         if int(flag.item()) == 0:
@@ -239,14 +271,22 @@ class MinSRGB300(PreconditionerGB300):
         self._st.mark("gram_head")
 
         def gram(T, sh):
-            _lib.call("vmc_sr_gram", _lib.ptr(Oc), code, Ns, Nd, Oc.stride(0), _lib.ptr(T), Ns, sh, 0, s)
+            tc = code == 1 and self.gram == "tensor"
+            if tc:
+                self._tc_gram(Oc, T, 1.0, None, sh, 0, dev)
+            else:
+                _lib.call("vmc_sr_gram", _lib.ptr(Oc), code, Ns, Nd, Oc.stride(0), _lib.ptr(T), Ns, sh, 0, s)
             self._st.mark("gram_dense")
-            _lib.call("vmc_gemm", 0, 1, Ns, Ns, Ng, 1.0 / Ns, _lib.ptr(G), G.stride(0), _lib.ptr(G), G.stride(0),
-                      None, code, 1.0, _lib.ptr(T), Ns, _lib.ptr(HH), Ns, 1, s)
+            if tc:
+                self._tc_gram(G, T, 1.0 / Ns, HH, 0.0, 1, dev)
+            else:
+                _lib.call("vmc_gemm", 0, 1, Ns, Ns, Ng, 1.0 / Ns, _lib.ptr(G), G.stride(0), _lib.ptr(G), G.stride(0),
+                          None, code, 1.0, _lib.ptr(T), Ns, _lib.ptr(HH), Ns, 1, s)
             _lib.call("vmc_sr_kron_correction", Ns, _lib.ptr(T), Ns, _lib.ptr(P), Nh, _lib.ptr(H), code, H.stride(0),
                       Nh, mu_sq, 1.0 / Ns, _lib.ptr(vwork), s)
             self._st.mark("gram_head")
 
+        gram.check = self._check_tc
         x, info = self._factor_solve(gram, E, Ebar, Ns, shift, dev, self._st)
         dp_d = torch.empty(Nd, dtype=torch.float64, device=dev)
         _lib.call("vmc_sr_update", _lib.ptr(Oc), code, Ns, Nd, Oc.stride(0), _lib.ptr(x), _lib.ptr(dp_d), s)

@@ -291,7 +291,8 @@ class OnlineProposalTraining:
     last ``buffer`` samples), and every ``every`` steps the proposal trains
     for ``epochs`` epochs over the buffer.  ``then`` is called afterwards with
     the same info (to chain the caller's own callback).  ``train_seconds``
-    accumulates the training wall time (synchronised) for the ESS accounting."""
+    accumulates the training time for the ESS accounting, measured like the
+    samplers' times: CUDA events on the current stream around each session."""
 
     def __init__(self, proposal, model, every=10, epochs=2, batch=4096, then=None):
         self.proposal, self.model = proposal, model
@@ -306,11 +307,13 @@ class OnlineProposalTraining:
         self.proposal.record(self.model)
         self.steps += 1
         if self.steps % self.every == 0:
-            torch.cuda.synchronize(self.proposal.device)
-            t0 = time.time()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
             self.last_loss = self.proposal.train(epochs=self.epochs, batch=self.batch)
-            torch.cuda.synchronize(self.proposal.device)
-            self.train_seconds += time.time() - t0
+            e1.record()
+            e1.synchronize()
+            self.train_seconds += e0.elapsed_time(e1) / 1e3
             self.sessions += 1
         if self.then is not None:
             self.then(info)
