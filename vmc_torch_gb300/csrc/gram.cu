@@ -10,17 +10,18 @@
 // 2^-24), and the product x_i x_j is taken as the six terms
 //   hi hi + hi mid + mid hi + hi lo + lo hi + mid mid
 // (the three dropped terms are below 2^-24 relative).  The products are exact
-// in the FP32 accumulator; the accumulator is drained into the FP64 result
-// every 2048 columns of K, so FP32 rounding only acts on partial sums of 2048
-// terms.
+// in FP32.  The leading term hi hi accumulates in one TMEM accumulator and the
+// five small terms (2^-8 of it and below) in a second, so the FP32 rounding of
+// the large running sum happens once per K=16 step of a single product; both
+// are drained into the FP64 result every 2048 columns of K.
 //
 // Tile: 128 x 128 outputs per CTA, lower triangle of tiles only (the upper
 // triangle is written as the mirror image).  K atoms of 64 BF16 (128 bytes per
 // row) are staged by TMA (SWIZZLE_128B) through a 2-stage pipeline; each stage
 // holds the three planes of the 128 rows of both operands (96 KB).  Warp 0
 // issues the copies, warp 1 (one thread) the tcgen05 MMAs into two TMEM
-// accumulators (2 x 128 columns) used alternately per K chunk, warps 2..5 add
-// each finished chunk into T.
+// buffers used alternately per K chunk (each 2 x 128 columns: leading and
+// small products), warps 2..5 add each finished chunk into T.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
@@ -98,7 +99,7 @@ __global__ void __launch_bounds__(GR_THREADS, 1)
     tc::fence_mbar_init();
     tc::prefetch_tmap(&tmX);
   }
-  if (warp == 0) tc::tmem_alloc(tslot, 256);
+  if (warp == 0) tc::tmem_alloc(tslot, 512);
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
@@ -135,7 +136,7 @@ __global__ void __launch_bounds__(GR_THREADS, 1)
           break;
         }
         tc::fence_after_sync();
-        const uint32_t dt = tbase + (uint32_t)(buf * GT);
+        const uint32_t dt = tbase + (uint32_t)(buf * 2 * GT);   // leading products; small ones at + GT
         const int a0 = c * CHUNK_ATOMS, a1 = min(ga.n_atoms, a0 + CHUNK_ATOMS);
         bool ok = true;
         for (int a = a0; a < a1; ++a) {
@@ -149,7 +150,8 @@ __global__ void __launch_bounds__(GR_THREADS, 1)
             for (int kk = 0; kk < 4; ++kk) {
               const uint64_t ad = tc::sdesc_sw128(tc::smem_u32(st + pa[q] * PLANE) + kk * 32);
               const uint64_t bd = tc::sdesc_sw128(tc::smem_u32(st + (3 + pb[q]) * PLANE) + kk * 32);
-              tc::mma_bf16(dt, ad, bd, idesc, (a > a0 || q || kk) ? 1u : 0u);
+              if (q == 0) tc::mma_bf16(dt, ad, bd, idesc, (a > a0 || kk) ? 1u : 0u);
+              else tc::mma_bf16(dt + GT, ad, bd, idesc, (a > a0 || q > 1 || kk) ? 1u : 0u);
             }
           }
           tc::mma_commit(&empty[s]);   // the stage is free once these MMAs have read it
@@ -173,15 +175,17 @@ __global__ void __launch_bounds__(GR_THREADS, 1)
       const bool last = c == n_chunks - 1;
 #pragma unroll 1
       for (int cc = 0; cc < GT / 32; ++cc) {
-        float v[32];
-        tc::tmem_ld32(tbase + (uint32_t)(buf * GT) + ((uint32_t)(quad * 32) << 16) + (uint32_t)(cc * 32), v);
+        float v[32], w[32];
+        const uint32_t ta = tbase + (uint32_t)(buf * 2 * GT) + ((uint32_t)(quad * 32) << 16) + (uint32_t)(cc * 32);
+        tc::tmem_ld32(ta, v);
+        tc::tmem_ld32(ta + GT, w);
         if (!live) continue;
 #pragma unroll
         for (int q = 0; q < 32; ++q) {
           const int64_t gj = (int64_t)bj * GT + cc * 32 + q;
           if (gj >= ga.n || (bi == bj && gj > gi)) continue;
           double* t = ga.T + gi * ga.ldt + gj;
-          double add = ga.alpha * (double)v[q];
+          double add = ga.alpha * ((double)v[q] + (double)w[q]);
           if (ga.D) add *= ga.D[gi * ga.ldt + gj];
           double val = first ? add : *t + add;
           if (last && gj == gi) val += ga.shift;
@@ -196,7 +200,7 @@ __global__ void __launch_bounds__(GR_THREADS, 1)
   }
   tc::fence_before_sync();
   __syncthreads();
-  if (warp == 0) tc::tmem_dealloc(tbase, 256);
+  if (warp == 0) tc::tmem_dealloc(tbase, 512);
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 g_enc = nullptr;
