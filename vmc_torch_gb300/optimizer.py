@@ -131,11 +131,15 @@ class MinSRGB300(PreconditionerGB300):
     (centring, Gram blocks, Cholesky, triangular solves, update) in
     ``last_stages`` (milliseconds, CUDA events on the current stream)."""
 
-    def __init__(self, record_stages=False, gram="tensor"):
-        """gram: "tensor" forms the Gram blocks of FP32 O on the tensor cores
-        (vmc_sr_gram_tc: BF16 three-way split, six products, FP32 partial sums
-        drained into FP64); "cuda" keeps them on the CUDA cores with
-        compensated FP32 accumulation.  FP64 O always uses FP64 arithmetic."""
+    def __init__(self, record_stages=False, gram="cuda"):
+        """gram: "cuda" (default) forms the Gram blocks of FP32 O on the CUDA
+        cores with compensated (double-float) accumulation, FP64-level.
+        "tensor" forms them on the tensor cores (vmc_sr_gram_tc: BF16
+        three-way split, six products, FP32 partial sums drained into FP64
+        every 2048 columns): ~6x faster, but its entries carry ~5e-6 of the
+        largest diagonal entry in rounding, so use it only where the diagonal
+        shift is well above that (at 16384 samples and shift 1e-4 the rounding
+        makes T indefinite).  FP64 O always uses FP64 arithmetic."""
         if gram not in ("tensor", "cuda"):
             raise ValueError("gram must be 'tensor' or 'cuda'")
         self.record_stages = record_stages
