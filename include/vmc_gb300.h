@@ -137,13 +137,16 @@ int vmc_nnbf_eval(int prec, const void* const* net_ptrs, int n_sites, int nf, in
  * u64) counts evaluated proposals; stage_ms[4] / stage_launches[4] (HOST arrays)
  * accumulate the device time of the [prep, hidden layer, backflow GEMM, LU]
  * launches, measured with CUDA events on `stream` (the call then synchronises
- * the stream before returning). */
+ * the stream before returning).  compact_ws (nullable, 16-byte aligned,
+ * 256 + 4 B rounded up to 16 + 16 B bytes): with it, mixed precision and 64
+ * orbitals, each edge's GEMMs and LU run over the walkers whose proposal
+ * changes them only (compacted on the device; results identical). */
 int vmc_nnbf_sweep(int prec, const void* const* net_ptrs, int n_sites, int nf, int hidden, double bf_scale,
                    uint64_t* occ, int64_t B, const int32_t* edges, int n_edges, int n_sweeps, float hopping_rate,
                    uint64_t seed, uint64_t sweep_offset, const float* r_move, const uint8_t* r_bit, const float* r_acc,
                    void* z0, double* sign, double* logabs, int32_t* n_acc, uint64_t* prop_occ, void* rec, void* H1,
                    void* H2, void* A, int* d_err, unsigned long long* d_n_eval, float* stage_ms, int* stage_launches,
-                   void* stream);
+                   void* compact_ws, void* stream);
 /* Local-energy support (vmc_torch/GPU/vmc_utils.py:322-476): per-walker count
  * of valid hop terms, then the (walker, hop-term) pair list at offsets offs
  * (B+1, exclusive scan of the counts).  Hop term = 2*edge + (0 up, 1 down). */

@@ -44,7 +44,7 @@ SIGNATURES = {
     "vmc_slater_logpsi_grad": [P, P, I64, I32, I32, P, I64, P],
     "vmc_nnbf_eval": [I32, P, I32, I32, I32, F64, P, I64, P, P, P, P, P, P, P, P],
     "vmc_nnbf_sweep": [I32, P, I32, I32, I32, F64, P, I64, P, I32, I32, F32, U64, U64, P, P, P, P, P, P, P, P, P,
-                       P, P, P, P, P, P, P, P],
+                       P, P, P, P, P, P, P, P, P],
     "vmc_nnbf_eval_noalloc": [P, I32, I32, I32, F64, P, I64, P, P, P, P],
     "vmc_nnbf_hidden_layer": [P, I64, P, P, P, U64, I32, P, P],
     "vmc_check_finite": [P, P, I64, P, I32, I64, I64, P, P, P, P, P],

@@ -80,14 +80,25 @@ template <> __device__ __forceinline__ double gelu_t<double>(double x) { return 
 
 // Sweep prep for edge e of sweep s: proposal, proposed occupation, moves, h1.
 // Walkers [w_begin, w_end) of the B; arrays are indexed by the global walker.
+// Row compaction (cnt non-null): a walker whose proposal changes it takes the
+// next compact row of its group (atomic slot in *cnt, cleared before the
+// launch); its hidden activations go to that row of H1, the row's walker
+// (index within the group) to row_map and its proposed occupation to prop_c,
+// so that the GEMMs and the LU run over the changed walkers only.  A row's
+// arithmetic does not depend on which rows share its tile or warp, so the
+// results do not depend on the slot order.
 template <typename T>
 __global__ void k_prep_sweep(int64_t B, int64_t w_begin, int64_t w_end, int N, const uint64_t* __restrict__ occ,
                              const int32_t* __restrict__ edges, int e, int s_local, int E, float hop_rate,
                              uint64_t seed, uint64_t sweep_idx, const float* __restrict__ rm,
                              const uint8_t* __restrict__ rb, const float* __restrict__ ra, const T* __restrict__ z0,
                              const T* __restrict__ w0t, uint64_t* __restrict__ prop_occ, PropRec* __restrict__ rec,
-                             void* __restrict__ H1) {
+                             void* __restrict__ H1, int* __restrict__ cnt, int32_t* __restrict__ row_map,
+                             uint64_t* __restrict__ prop_c, int* __restrict__ cnt_next) {
   const int lane = threadIdx.x & 31;
+  // the counter of the next edge: its previous users (the launches of the
+  // edge before this one) have finished, as they precede this launch
+  if (cnt_next && blockIdx.x == 0 && threadIdx.x == 0) *cnt_next = 0;
   const int64_t w = w_begin + (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
   if (w >= w_end) return;
   uint64_t up = occ[2 * w], dn = occ[2 * w + 1];
@@ -120,6 +131,17 @@ __global__ void k_prep_sweep(int64_t B, int64_t w_begin, int64_t w_end, int N, c
     rec[w] = r;
   }
   if (!r.flag) return;
+  int64_t hrow = w;
+  if (cnt) {
+    int slot = 0;
+    if (lane == 0) {
+      slot = atomicAdd(cnt, 1);
+      row_map[w_begin + slot] = (int32_t)(w - w_begin);
+      prop_c[2 * (w_begin + slot)] = up;
+      prop_c[2 * (w_begin + slot) + 1] = dn;
+    }
+    hrow = w_begin + __shfl_sync(VMC_FULL_MASK, slot, 0);
+  }
   T h[8];
 #pragma unroll
   for (int q = 0; q < 8; ++q) h[q] = z0[w * HID + lane * 8 + q];
@@ -129,7 +151,7 @@ __global__ void k_prep_sweep(int64_t B, int64_t w_begin, int64_t w_end, int N, c
   }
 #pragma unroll
   for (int q = 0; q < 8; ++q) h[q] = gelu_t<T>(h[q]);
-  H1Store<T>::store(H1, w, lane, h);
+  H1Store<T>::store(H1, hrow, lane, h);
 }
 
 // z0 = b0 + sum of W0 columns of the occupied orbitals (from scratch); h1 -> H1.
@@ -225,6 +247,8 @@ struct EpiArgs {
   // timeout path, vmc_nnbf_hidden_layer)
   uint64_t wait_ns;
   int skip_loads;
+  // compacted rows: the row count is *rows_dev (device), at most `rows`
+  const int* rows_dev;
 };
 
 template <int EPI>
@@ -243,6 +267,11 @@ __global__ void __launch_bounds__(128, 1)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int row0 = blockIdx.x * TM;
   const int brow0 = blockIdx.y * TN;
+  if (ea.rows_dev) {   // uniform over the CTA, before any barrier or allocation
+    const int rr = *ea.rows_dev;
+    if (row0 >= rr) return;
+    rows = rows < rr ? rows : rr;
+  }
   if (threadIdx.x == 0) {
     tc::mbar_init(&bars[0], 1);
     tc::mbar_init(&bars[1], 1);
@@ -366,6 +395,9 @@ struct PBArgs {
   float* Aout;              // (R, nf, nf)
   float scale;
   int n_sites, nf, R, n_tiles, n_items;
+  // compacted rows: the row count is clamp(*rows_dev - rows_off, 0, R) (device)
+  const int* rows_dev;
+  int64_t rows_off;
 };
 
 __global__ void __launch_bounds__(PB_THREADS, 1)
@@ -387,9 +419,17 @@ __global__ void __launch_bounds__(PB_THREADS, 1)
   float* cM = (float*)(sm + SMEM_A + SMEM_B + 256);
   float* cO = cM + TN;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int per = (pa.n_items + gridDim.x - 1) / gridDim.x;
+  int R = pa.R, n_tiles = pa.n_tiles, n_items = pa.n_items;
+  if (pa.rows_dev) {   // the same value in every thread: all roles walk the same items
+    const int64_t rr = (int64_t)*pa.rows_dev - pa.rows_off;
+    R = rr < 0 ? 0 : (rr < R ? (int)rr : R);
+    const int n_groups = pa.n_items / pa.n_tiles;
+    n_tiles = (R + TM - 1) / TM;
+    n_items = n_groups * n_tiles;
+  }
+  const int per = (n_items + gridDim.x - 1) / gridDim.x;
   const int it0 = blockIdx.x * per;
-  const int it1 = min(pa.n_items, it0 + per);
+  const int it1 = min(n_items, it0 + per);
   if (threadIdx.x == 0) {
     tc::mbar_init(bfull, 1);
     tc::mbar_init(bempty, 1);
@@ -410,7 +450,7 @@ __global__ void __launch_bounds__(PB_THREADS, 1)
       if (lane == 0) {  // ---------------- TMA producer ----------------
         int cur_g = -1, ng = 0;
         for (int it = it0, i = 0; it < it1 && !*abort_flag; ++it, ++i) {
-          const int g = it / pa.n_tiles, t = it - g * pa.n_tiles;
+          const int g = it / n_tiles, t = it - g * n_tiles;
           if (g != cur_g) {
             if (cur_g >= 0 && !tc::mbar_wait(bempty, (ng - 1) & 1)) { *abort_flag = 1; atomicExch(err, VMC_ERR_TIMEOUT); break; }
             tc::mbar_arrive_expect_tx(bfull, SMEM_B);
@@ -430,7 +470,7 @@ __global__ void __launch_bounds__(PB_THREADS, 1)
         constexpr uint32_t idesc = tc::idesc_bf16_f32(TM, TN);
         int cur_g = -1, ng = 0;
         for (int it = it0, i = 0; it < it1 && !*abort_flag; ++it, ++i) {
-          const int g = it / pa.n_tiles;
+          const int g = it / n_tiles;
           if (g != cur_g) {
             if (!tc::mbar_wait(bfull, ng & 1)) { *abort_flag = 1; atomicExch(err, VMC_ERR_TIMEOUT); break; }
             cur_g = g;
@@ -454,7 +494,7 @@ __global__ void __launch_bounds__(PB_THREADS, 1)
           }
           if (!ok) { *abort_flag = 1; atomicExch(err, VMC_ERR_TIMEOUT); break; }
           tc::mma_commit(&tfull[buf]);
-          const int gn = (it + 1 < it1) ? (it + 1) / pa.n_tiles : -2;
+          const int gn = (it + 1 < it1) ? (it + 1) / n_tiles : -2;
           if (gn != g) tc::mma_commit(bempty);  // B of group g no longer needed
         }
       }
@@ -463,7 +503,7 @@ __global__ void __launch_bounds__(PB_THREADS, 1)
       const int et = threadIdx.x - 64;   // 0..127
       int cur_g = -1;
       for (int it = it0, i = 0; it < it1; ++it, ++i) {
-        const int g = it / pa.n_tiles, t = it - g * pa.n_tiles;
+        const int g = it / n_tiles, t = it - g * n_tiles;
         if (g != cur_g) {
           asm volatile("bar.sync 1, 128;" ::: "memory");
           for (int q = et; q < TN; q += 128) { cM[q] = pa.mbase[g * TN + q]; cO[q] = pa.outb[g * TN + q]; }
@@ -476,7 +516,7 @@ __global__ void __launch_bounds__(PB_THREADS, 1)
         if (!ok) { if (lane == 0) { *abort_flag = 1; atomicExch(err, VMC_ERR_TIMEOUT); } break; }
         tc::fence_after_sync();
         const int64_t row = (int64_t)t * TM + quad * 32 + lane;
-        const bool live = row < pa.R;
+        const bool live = row < R;
         uint64_t up = 0, dn = 0;
         if (live) { up = pa.row_occ[2 * row]; dn = pa.row_occ[2 * row + 1]; }
         const int nf = pa.nf, N = pa.n_sites;
@@ -1080,7 +1120,21 @@ struct LdArgs {
   const int32_t* pairs;
   const double* coeff;
   double* term;
+  // compacted rows (accept mode): rows [0, clamp(*rows_dev - rows_off)) of
+  // the launch are the changed walkers row_map[rows_off + local]
+  const int* rows_dev;
+  int64_t rows_off;
+  const int32_t* row_map;
 };
+
+__device__ __forceinline__ int64_t ld_rows(const LdArgs& la, int64_t R) {
+  if (!la.rows_dev) return R;
+  const int64_t rr = (int64_t)*la.rows_dev - la.rows_off;
+  return rr < 0 ? 0 : (rr < R ? rr : R);
+}
+__device__ __forceinline__ int64_t ld_row(const LdArgs& la, int64_t row0, int64_t l) {
+  return la.row_map ? (int64_t)la.row_map[row0 + l] : row0 + l;
+}
 
 // What the evaluated row's log-determinant is used for: EVAL stores it, ELOC
 // forms the hop term, ACCEPT / ACCEPT_Q run the Metropolis(-Hastings) test and
@@ -1213,8 +1267,9 @@ __global__ void __launch_bounds__(128, LU_MIN_CTAS) k_logdet_pair(int64_t R, int
   extern __shared__ __align__(16) uint8_t lsm[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t base = (int64_t)blockIdx.x * 4;
+  const int64_t Reff = ld_rows(la, R);
   bool fl = false;
-  if (lane < 4 && base + lane < R) fl = ld_flag<MODE>(la, row0 + base + lane);
+  if (lane < 4 && base + lane < Reff) fl = la.rows_dev ? true : ld_flag<MODE>(la, row0 + base + lane);
   const unsigned mask = __ballot_sync(VMC_FULL_MASK, fl);
   const int n = __popc(mask);
   if (warp >= n) return;
@@ -1264,7 +1319,7 @@ __global__ void __launch_bounds__(128, LU_MIN_CTAS) k_logdet_pair(int64_t R, int
   }
   const int nd = paired ? 2 : 1;
 #pragma unroll 1
-  for (int k = 0; k < nd; ++k) ld_finish<float, MODE>(row0 + (k ? lp : l), k ? d1 : d0, la, lane);
+  for (int k = 0; k < nd; ++k) ld_finish<float, MODE>(ld_row(la, row0, k ? lp : l), k ? d1 : d0, la, lane);
 }
 
 // FP32 64 x 64 rows, two matrices a warp throughout: a CTA of 4 warps takes
@@ -1278,8 +1333,9 @@ __global__ void __launch_bounds__(128, LU_MIN_CTAS) k_logdet_dual(int64_t R, int
   extern __shared__ __align__(16) uint8_t lsm[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t base = (int64_t)blockIdx.x * 8;
+  const int64_t Reff = ld_rows(la, R);
   bool fl = false;
-  if (lane < 8 && base + lane < R) fl = ld_flag<MODE>(la, row0 + base + lane);
+  if (lane < 8 && base + lane < Reff) fl = la.rows_dev ? true : ld_flag<MODE>(la, row0 + base + lane);
   unsigned m = __ballot_sync(VMC_FULL_MASK, fl);
   for (int i = 0; i < 2 * warp; ++i) m &= m - 1u;
   if (!m) return;
@@ -1296,7 +1352,7 @@ __global__ void __launch_bounds__(128, LU_MIN_CTAS) k_logdet_dual(int64_t R, int
   Det d0, d1;
   warp_logdet_f32_pair(A, prow, sw, nd, d0, d1);
 #pragma unroll 1
-  for (int k = 0; k < nd; ++k) ld_finish<float, MODE>(row0 + (int64_t)sw[38 + k], k ? d1 : d0, la, lane);
+  for (int k = 0; k < nd; ++k) ld_finish<float, MODE>(ld_row(la, row0, (int64_t)sw[38 + k]), k ? d1 : d0, la, lane);
 }
 
 // per-walker local energy: U * doublons + segmented sum of the hop terms
@@ -1512,9 +1568,12 @@ int sweep_lanes() {
   return n;
 }
 
+// d_count / row_map (mixed precision, nf = 64): the rows are compacted, their
+// number *d_count on the device (at most R) and their walkers row_map.
 int launch_eval_rows(int prec, int64_t R, int N, int nf, const uint64_t* row_occ, const void* net, double scale,
                      const Work& wk, int* err, cudaStream_t st, int ldmode, const LdArgs& la,
-                     bool allow_pipe = true, bool concurrent = false) {
+                     bool allow_pipe = true, bool concurrent = false, const int* d_count = nullptr,
+                     const int32_t* row_map = nullptr) {
   const int n_orb = 2 * N;
   if (prec == 0) {
     const NetF32& n = *(const NetF32*)net;
@@ -1525,6 +1584,7 @@ int launch_eval_rows(int prec, int64_t R, int N, int nf, const uint64_t* row_occ
     EpiArgs e1{};
     e1.bias = n.b1;
     e1.out = (__nv_bfloat16*)wk.H2;
+    e1.rows_dev = d_count;
     dim3 g1((unsigned)((R + TM - 1) / TM), 1);
     STAGE_BEGIN(1);
     k_gemm_tc<EPI_GELU_BF16><<<g1, 128, GEMM_SMEM, st>>>(tH1, tW1, (int)R, e1, err);
@@ -1562,6 +1622,8 @@ int launch_eval_rows(int prec, int64_t R, int N, int nf, const uint64_t* row_occ
       pa.scale = (float)scale; pa.n_sites = N; pa.nf = nf; pa.R = (int)Rc;
       pa.n_tiles = (int)((Rc + TM - 1) / TM);
       pa.n_items = n_groups * pa.n_tiles;
+      pa.rows_dev = d_count;
+      pa.rows_off = c0;
       const int grid = pa.n_items < num_sms() ? pa.n_items : num_sms();
       cudaStream_t gs = pipe ? pipe->aux : st;
       if (pipe && ci >= 2 && cudaStreamWaitEvent(gs, pipe->lu[slot], 0) != cudaSuccess) return fail(VMC_ERR_CUDA);
@@ -1573,22 +1635,27 @@ int launch_eval_rows(int prec, int64_t R, int N, int nf, const uint64_t* row_occ
           return fail(VMC_ERR_CUDA);
       }
       STAGE_BEGIN(3);
+      LdArgs lc = la;
+      lc.rows_dev = d_count;
+      lc.rows_off = c0;
+      lc.row_map = row_map;
       const unsigned gl = (unsigned)((Rc + wpb - 1) / wpb);
       if (nf == 64 && !concurrent) {  // warp pairs share the tails (the orbital-matrix slot is scratch: the LU parks in it)
         const unsigned gp = (unsigned)((Rc + wpb - 1) / wpb);
         const size_t psmem = (size_t)wpb * LDP_WARP_WORDS * sizeof(float);
-        if (ldmode == LD_ACCEPT) k_logdet_pair<LD_ACCEPT><<<gp, 32 * wpb, psmem, st>>>(Rc, c0, Ac, la);
-        else if (ldmode == LD_EVAL) k_logdet_pair<LD_EVAL><<<gp, 32 * wpb, psmem, st>>>(Rc, c0, Ac, la);
-        else if (ldmode == LD_ACCEPT_Q) k_logdet_pair<LD_ACCEPT_Q><<<gp, 32 * wpb, psmem, st>>>(Rc, c0, Ac, la);
-        else k_logdet_pair<LD_ELOC><<<gp, 32 * wpb, psmem, st>>>(Rc, c0, Ac, la);
+        if (ldmode == LD_ACCEPT) k_logdet_pair<LD_ACCEPT><<<gp, 32 * wpb, psmem, st>>>(Rc, c0, Ac, lc);
+        else if (ldmode == LD_EVAL) k_logdet_pair<LD_EVAL><<<gp, 32 * wpb, psmem, st>>>(Rc, c0, Ac, lc);
+        else if (ldmode == LD_ACCEPT_Q) k_logdet_pair<LD_ACCEPT_Q><<<gp, 32 * wpb, psmem, st>>>(Rc, c0, Ac, lc);
+        else k_logdet_pair<LD_ELOC><<<gp, 32 * wpb, psmem, st>>>(Rc, c0, Ac, lc);
       } else if (nf == 64) {  // two matrices a warp (concurrent walker groups fill the SMs)
         const unsigned gp = (unsigned)((Rc + 2 * wpb - 1) / (2 * wpb));
         const size_t psmem = (size_t)wpb * LDP_WARP_WORDS * sizeof(float);
-        if (ldmode == LD_ACCEPT) k_logdet_dual<LD_ACCEPT><<<gp, 32 * wpb, psmem, st>>>(Rc, c0, Ac, la);
-        else if (ldmode == LD_EVAL) k_logdet_dual<LD_EVAL><<<gp, 32 * wpb, psmem, st>>>(Rc, c0, Ac, la);
-        else if (ldmode == LD_ACCEPT_Q) k_logdet_dual<LD_ACCEPT_Q><<<gp, 32 * wpb, psmem, st>>>(Rc, c0, Ac, la);
-        else k_logdet_dual<LD_ELOC><<<gp, 32 * wpb, psmem, st>>>(Rc, c0, Ac, la);
+        if (ldmode == LD_ACCEPT) k_logdet_dual<LD_ACCEPT><<<gp, 32 * wpb, psmem, st>>>(Rc, c0, Ac, lc);
+        else if (ldmode == LD_EVAL) k_logdet_dual<LD_EVAL><<<gp, 32 * wpb, psmem, st>>>(Rc, c0, Ac, lc);
+        else if (ldmode == LD_ACCEPT_Q) k_logdet_dual<LD_ACCEPT_Q><<<gp, 32 * wpb, psmem, st>>>(Rc, c0, Ac, lc);
+        else k_logdet_dual<LD_ELOC><<<gp, 32 * wpb, psmem, st>>>(Rc, c0, Ac, lc);
       } else {
+        // no compaction with 32 orbitals (the caller passes none)
         if (ldmode == LD_ACCEPT) k_logdet<float, 32, LD_ACCEPT><<<gl, 32 * wpb, lsmem, st>>>(Rc, c0, nf, Ac, la);
         else if (ldmode == LD_EVAL) k_logdet<float, 32, LD_EVAL><<<gl, 32 * wpb, lsmem, st>>>(Rc, c0, nf, Ac, la);
         else if (ldmode == LD_ACCEPT_Q) k_logdet<float, 32, LD_ACCEPT_Q><<<gl, 32 * wpb, lsmem, st>>>(Rc, c0, nf, Ac, la);
@@ -1683,10 +1750,11 @@ int vmc_nnbf_sweep(int prec, const void* const* net_ptrs, int n_sites, int nf, i
                    uint64_t seed, uint64_t sweep_offset, const float* r_move, const uint8_t* r_bit, const float* r_acc,
                    void* z0, double* sign, double* logabs, int32_t* n_acc, uint64_t* prop_occ, void* rec, void* H1,
                    void* H2, void* A, int* d_err, unsigned long long* d_n_eval, float* stage_ms, int* stage_launches,
-                   void* stream) {
+                   void* compact_ws, void* stream) {
   int st0 = check_shape(prec, n_sites, nf, hidden);
   if (st0) return st0;
   if (B < 0 || n_edges < 0 || n_sweeps < 0) return VMC_ERR_ARGS;
+  if (compact_ws && ((uintptr_t)compact_ws & 15) != 0) return VMC_ERR_ARGS;
   if ((r_move != nullptr) != (r_acc != nullptr) || (r_move != nullptr) != (r_bit != nullptr)) return VMC_ERR_ARGS;
   if (B == 0 || n_edges == 0 || n_sweeps == 0) return VMC_OK;
   if (!net_ptrs || !occ || !edges || !z0 || !sign || !logabs || !n_acc || !prop_occ || !rec || !H1 || !H2 || !A ||
@@ -1722,6 +1790,17 @@ int vmc_nnbf_sweep(int prec, const void* const* net_ptrs, int n_sites, int nf, i
   g_timer.acc = stage_ms;
   g_timer.cnt = stage_launches;
   g_timer.used = 0;
+  // row compaction (mixed precision, 64 orbitals): workspace = two counters
+  // per walker group (alternating edges) | row_map (B int32) | prop_c (B x 2 u64)
+  int* ccnt = nullptr;
+  int32_t* cmap = nullptr;
+  uint64_t* cprop = nullptr;
+  if (compact_ws && prec == 0 && nf == 64) {
+    ccnt = (int*)compact_ws;
+    cmap = (int32_t*)((char*)compact_ws + 256);
+    cprop = (uint64_t*)((char*)compact_ws + 256 + (((size_t)B * 4 + 15) & ~(size_t)15));
+    if (cudaMemsetAsync(ccnt, 0, 2 * ChunkPipe::kLanes * sizeof(int), st) != cudaSuccess) return VMC_ERR_CUDA;
+  }
   // walker groups on their own streams (mixed precision, untimed stages, B >= 2 chunks)
   ChunkPipe* pipe = nullptr;
   int G = 1;
@@ -1756,11 +1835,16 @@ int vmc_nnbf_sweep(int prec, const void* const* net_ptrs, int n_sites, int nf, i
       const unsigned gwg = (unsigned)(((w1 - w0) * 32 + 255) / 256);
       for (int s = 0; s < n_sweeps; ++s) {
         for (int e = 0; e < n_edges; ++e) {
+          const int par = (s * n_edges + e) & 1;
+          int* cn = ccnt ? ccnt + 2 * g + par : nullptr;
+          int* cx = ccnt ? ccnt + 2 * g + (par ^ 1) : nullptr;
           k_prep_sweep<float><<<gwg, 256, 0, gs>>>(B, w0, w1, n_sites, occ, edges, e, s, n_edges, hopping_rate, seed,
                                                    sweep_offset + (uint64_t)s, r_move, r_bit, r_acc,
-                                                   (const float*)z0, nf32.w0t, prop_occ, (PropRec*)rec, H1);
-          int rc = launch_eval_rows(prec, w1 - w0, n_sites, nf, prop_occ + 2 * w0, net, bf_scale, wg, d_err, gs,
-                                    LD_ACCEPT, lg, /*allow_pipe=*/false, /*concurrent=*/true);
+                                                   (const float*)z0, nf32.w0t, prop_occ, (PropRec*)rec, H1, cn, cmap,
+                                                   cprop, cx);
+          int rc = launch_eval_rows(prec, w1 - w0, n_sites, nf, cn ? cprop + 2 * w0 : prop_occ + 2 * w0, net,
+                                    bf_scale, wg, d_err, gs, LD_ACCEPT, lg, /*allow_pipe=*/false,
+                                    /*concurrent=*/true, cn, cn ? cmap + w0 : nullptr);
           if (rc) {
             // kernels already queued on this group's stream still write the
             // caller's buffers: the caller's stream waits for them all the same
@@ -1780,18 +1864,22 @@ int vmc_nnbf_sweep(int prec, const void* const* net_ptrs, int n_sites, int nf, i
   }
   for (int s = 0; s < n_sweeps; ++s) {
     for (int e = 0; e < n_edges; ++e) {
+      const int par = (s * n_edges + e) & 1;
+      int* cn = ccnt ? ccnt + par : nullptr;
+      int* cx = ccnt ? ccnt + (par ^ 1) : nullptr;
       STAGE_BEGIN(0);
       if (prec == 0)
         k_prep_sweep<float><<<gw, 256, 0, st>>>(B, 0, B, n_sites, occ, edges, e, s, n_edges, hopping_rate, seed,
                                                 sweep_offset + (uint64_t)s, r_move, r_bit, r_acc, (const float*)z0,
-                                                nf32.w0t, prop_occ, (PropRec*)rec, H1);
+                                                nf32.w0t, prop_occ, (PropRec*)rec, H1, cn, cmap, cprop, cx);
       else
         k_prep_sweep<double><<<gw, 256, 0, st>>>(B, 0, B, n_sites, occ, edges, e, s, n_edges, hopping_rate, seed,
                                                  sweep_offset + (uint64_t)s, r_move, r_bit, r_acc,
-                                                 (const double*)z0, nf64.w0t, prop_occ, (PropRec*)rec, H1);
+                                                 (const double*)z0, nf64.w0t, prop_occ, (PropRec*)rec, H1, nullptr,
+                                                 nullptr, nullptr, nullptr);
       STAGE_END(0);
-      int rc = launch_eval_rows(prec, B, n_sites, nf, prop_occ, net, bf_scale, Work{H1, H2, A}, d_err, st,
-                                LD_ACCEPT, la);
+      int rc = launch_eval_rows(prec, B, n_sites, nf, cn ? cprop : prop_occ, net, bf_scale, Work{H1, H2, A}, d_err,
+                                st, LD_ACCEPT, la, true, false, cn, cn ? cmap : nullptr);
       if (rc) { g_timer.acc = nullptr; return rc; }
     }
   }

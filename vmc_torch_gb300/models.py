@@ -385,6 +385,8 @@ class NNBF_GB300(WavefunctionModel_GB300):
         self.precision = precision
         self._net_cache = None
         self.refresh_each_sweep = True
+        # sweeps evaluate only the walkers whose proposal changes them
+        self.compact_rows = True
 
     # ---- device copies of the parameters in kernel layout ----
     def net(self, device):
@@ -460,7 +462,18 @@ class NNBF_GB300(WavefunctionModel_GB300):
                   _lib.ptr(x["z0"]), _lib.ptr(st.sign), _lib.ptr(st.logabs), _lib.ptr(st.n_acc),
                   _lib.ptr(x["prop_occ"]), _lib.ptr(x["rec"]), _lib.ptr(x["H1"]), _lib.ptr(x["H2"]),
                   _lib.ptr(x["A"]), _lib.ptr(x["err"]), *self._instr_args(instrument, st.device),
-                  _lib.stream_of(st.device))
+                  _lib.ptr(self._compact_ws(st)), _lib.stream_of(st.device))
+
+    def _compact_ws(self, st):
+        """Row-compaction workspace of the mixed 64-orbital sweep (None: off)."""
+        if self.precision != "mixed" or self.n_fermions != 64 or not self.compact_rows:
+            return None
+        ws = st.extra.get("compact")
+        if ws is None:
+            n = 256 + ((4 * st.B + 15) // 16) * 16 + 16 * st.B
+            ws = torch.empty(n, dtype=torch.uint8, device=st.device)
+            st.extra["compact"] = ws
+        return ws
 
     @staticmethod
     def _instr_args(instrument, device):
