@@ -617,9 +617,9 @@ def run_gb300(args):
     dom = int(np.argmax(stage_ms))
     kern_flops = [0.0, l1_flops, bf_flops, lu_flops]
     achieved = kern_flops[dom] / (stage_ms[dom] / 1e3) / 1e12
-    # DRAM bytes per LU launch (4096-row chunk) from one ncu capture (cold cache) of the
-    # kernel the per-kernel pass times: dram read 52.57 MB + write 0.07 MB
-    lu_traffic = 52.568832e6 + 0.067328e6 if dom == 3 else None
+    # DRAM bytes per LU launch (4096-row chunk, compacted rows) from one ncu capture
+    # (cold cache) of the kernel the per-kernel pass times: read 52.58 MB + write 0.02 MB
+    lu_traffic = 52.583936e6 + 0.016896e6 if dom == 3 else None
     roofline = {"bound": "tensor", "achieved": achieved, "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
                 "frac": achieved / pk["bf16_tflops"], "traffic": lu_traffic,
                 "traffic_note": "ncu dram__bytes_read+write per 4096-row LU launch, cold-cache capture",
