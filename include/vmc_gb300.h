@@ -356,6 +356,47 @@ int vmc_peps_local_energy(int prec, const void* tensors, int Lx, int Ly, int D, 
 int vmc_peps_logpsi_grad(int prec, const void* tensors, int Lx, int Ly, int D, const uint64_t* occ, int64_t B,
                          void* O, int64_t ldo, void* work, int64_t work_rows, void* stream);
 
+/* ---- fPEPS with the reference's chi-truncated boundary contraction
+ * (fPEPS_Model_GPU.amplitude / log_amplitude, vmc_torch/GPU/models/pureTNS.py:81-146:
+ * contract_boundary_from_xmin_ over rows [0, Lx/2-1] and _from_xmax_ over
+ * [Lx/2, Lx-1] with max_bond = chi, cutoff 0, then the two boundaries contracted).
+ * Same tensors, sign convention and (sign, logabs) semantics as vmc_peps_*.
+ * Each side's boundary is kept as the full vector over its D^Ly open legs; a row
+ * is absorbed exactly and the compression after it (left-to-right QR, right-to-left
+ * truncated SVD) is applied as the best rank-chi truncations across cuts
+ * Ly-1, ..., 1 that static rank bounds cannot rule out (Gram matrix of the smaller
+ * side, Z2 parity blocks, Jacobi eigenvectors).  Supported: Lx even >= 2,
+ * D in {2, 4}, D^Ly <= 4096, Lx * Ly <= 64, chi >= 1 (else VMC_ERR_UNSUPPORTED).
+ * work: *bytes from vmc_peps_chi_work_bytes(prec, Lx, Ly, D, chi, work_rows, bytes)
+ * of device memory (256-byte aligned) for chunks of work_rows walkers (or hop
+ * terms).
+ * vmc_peps_chi_schedule     — cuts[a] (a < Lx/2): bit k set when cut k (after k
+ *                             columns) is truncated after the a-th absorbed row of
+ *                             a side; all zero means the contraction is exact.
+ * vmc_peps_chi_eval         — forward_log of R configurations.
+ * vmc_peps_chi_sweep        — Metropolis sweeps with the proposals, random stream
+ *                             and acceptance of vmc_peps_sweep; per edge every
+ *                             walker's proposal rebuilds only the touched sides.
+ *                             sign/logabs are recomputed for the walkers first.
+ *                             d_n_eval (nullable) += evaluated proposals, side
+ *                             states built.
+ * vmc_peps_chi_local_energy — E_loc with pairs/offs from vmc_nnbf_conn_count/pairs;
+ *                             offs_host is a host copy of offs (B + 1 entries);
+ *                             term (P) receives the hop terms. */
+int vmc_peps_chi_work_bytes(int prec, int Lx, int Ly, int D, int chi, int64_t work_rows, int64_t* bytes);
+int vmc_peps_chi_schedule(int Lx, int Ly, int D, int chi, uint32_t* cuts, int max_rows);
+int vmc_peps_chi_eval(int prec, const void* tensors, int Lx, int Ly, int D, int chi, const uint64_t* occ, int64_t R,
+                      double* sign, double* logabs, void* work, int64_t work_rows, void* stream);
+int vmc_peps_chi_sweep(int prec, const void* tensors, int Lx, int Ly, int D, int chi, uint64_t* occ, int64_t B,
+                       const int32_t* edges, int n_edges, int n_sweeps, float hopping_rate, uint64_t seed,
+                       uint64_t sweep_offset, const float* r_move, const uint8_t* r_bit, const float* r_acc,
+                       double* sign, double* logabs, int32_t* n_acc, uint64_t* d_n_eval, void* work,
+                       int64_t work_rows, void* stream);
+int vmc_peps_chi_local_energy(int prec, const void* tensors, int Lx, int Ly, int D, int chi, const uint64_t* occ,
+                              int64_t B, const int32_t* edges, double t, double U, const int32_t* pairs,
+                              const int32_t* offs, const int32_t* offs_host, int64_t P, double* term, double* eloc,
+                              void* work, int64_t work_rows, void* stream);
+
 /* ---- Point-group symmetry projection with fermionic signs
  * (FermionSymmetryProjectedModel, vmc_torch/GPU/models/symmetry.py:770-1136) ----
  * psi_r(n) = (1/G) sum_g sign(g, n) chi_r(g) psi(n[perm_g]).

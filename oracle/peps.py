@@ -296,7 +296,77 @@ def amp_boundary_chi(T, x, chi):
     return g * float(E[0, 0])
 
 
-def logamp(T, X, method="rows"):
+def chi_schedule(Lx, Ly, D, chi):
+    """Cuts truncated after each absorbed row of one side (absorption order),
+    from static bounds on the Schmidt rank: a row multiplies the bond across
+    cut k by D, the rank never exceeds min(D^k, D^(Ly-k)), truncating cut k to
+    chi bounds cut k-1 by D*chi.  Cuts whose bound is <= chi need no SVD (the
+    truncation is the identity there).  Rows before the second are never
+    compressed (amp_boundary_chi starts from the bare first row)."""
+    b = [1] * (Ly + 1)
+    out = []
+    for a in range(Lx // 2):
+        for k in range(1, Ly):
+            b[k] = min(b[k] * D, D ** k, D ** (Ly - k))
+        cuts = []
+        if a >= 1:
+            for k in range(Ly - 1, 0, -1):
+                if b[k] > chi:
+                    cuts.append(k)
+                    b[k] = chi
+                    if k > 1:
+                        b[k - 1] = min(b[k - 1], D * chi)
+        out.append(cuts)
+    return out
+
+
+def _truncate_cut(psi, Ly, D, k, chi):
+    """Best rank-chi approximation of the state psi (D^Ly, column 0 most
+    significant) across the cut after k columns."""
+    M = psi.reshape(D ** k, D ** (Ly - k))
+    u, s, vh = np.linalg.svd(M, full_matrices=False)
+    r = min(chi, s.size)
+    return ((u[:, :r] * s[:r]) @ vh[:r]).reshape(-1)
+
+
+def amp_state_chi(T, x, chi, with_norms=False):
+    """amp_boundary_chi restated on the full boundary state: each side's
+    boundary is kept as a vector over the D^Ly open legs, a row is absorbed
+    exactly, and the compression (left-to-right QR, right-to-left truncated
+    SVD) becomes the sequence of best rank-chi truncations across cuts
+    Ly-1, ..., 1 of that vector -- in the canonical sweep the SVD at cut k is
+    the Schmidt decomposition of the whole current state across that cut.
+    The algorithm of the GPU kernels (vmc_peps_chi_*)."""
+    g, A = sign_rule(T, x)
+    Lx, Ly, D = A.shape[0], A.shape[1], A.shape[2]
+    sched = chi_schedule(Lx, Ly, D, chi)
+
+    def side(rows, top):
+        psi = np.zeros(D ** Ly)
+        psi[0] = 1.0
+        for a, r in enumerate(rows):
+            W = psi.reshape((D,) * Ly)[..., None] * np.eye(D)[0]       # (d_0..d_{Ly-1}, h)
+            for c in range(Ly):
+                t = A[r, c] if top else A[r, c].transpose(0, 3, 2, 1)   # (h, old, h', new)
+                W = np.moveaxis(W, c, -2)
+                W = np.einsum("...oh,hopn->...np", W, t)
+                W = np.moveaxis(W, -2, c)
+            psi = W[..., 0].reshape(-1)
+            for k in sched[a]:
+                psi = _truncate_cut(psi, Ly, D, k, chi)
+        return psi
+
+    top = side(range(0, Lx // 2), True)
+    bot = side(range(Lx - 1, Lx // 2 - 1, -1), False)
+    if with_norms:  # (psi, |top| |bot|): the scale of the final overlap's cancellation
+        return g * float(top @ bot), float(np.linalg.norm(top) * np.linalg.norm(bot))
+    return g * float(top @ bot)
+
+
+def logamp(T, X, method="rows", chi=None):
+    if method == "chi":
+        a = np.array([amp_state_chi(T, x, chi) for x in np.asarray(X)])
+        return np.sign(a), np.log(np.maximum(np.abs(a), 1e-300))
     f = {"rows": amp_rows, "brute": amp_bruteforce, "grassmann": amp_grassmann}[method]
     a = np.array([f(T, x) for x in np.asarray(X)])
     return np.sign(a), np.log(np.maximum(np.abs(a), 1e-300))

@@ -44,3 +44,28 @@ def test_truncated_boundary_converges_6x6():
     ex = peps.amp_rows(T, x)
     np.testing.assert_allclose(peps.amp_boundary_chi(T, x, 64), ex, rtol=1e-11)
     assert abs(peps.amp_boundary_chi(T, x, 16) / ex - 1) > 1e-3
+
+
+@pytest.mark.parametrize("Lx,Ly,D,chi", [(4, 4, 4, 8), (4, 4, 4, 3), (6, 6, 4, 16), (6, 6, 4, 8), (6, 4, 4, 8),
+                                         (4, 6, 4, 8), (6, 6, 2, 4)])
+def test_state_truncation_equals_mps_protocol(Lx, Ly, D, chi):
+    """The GPU kernels' formulation (full boundary state, best rank-chi
+    truncations across the scheduled cuts) equals the boundary-MPS protocol
+    (left-to-right QR, right-to-left truncated SVD after each absorbed row)."""
+    T = peps.init_tensors(Lx, Ly, D, seed=3)
+    N = Lx * Ly
+    n = N // 2 - 1 if N > 8 else N // 2
+    X = lattice.random_initial_configs(3, N, n, n, seed=1)
+    for x in X:
+        a = peps.amp_boundary_chi(T, x, chi)
+        b = peps.amp_state_chi(T, x, chi)
+        assert abs(a - b) <= 1e-11 * abs(a)
+
+
+def test_chi_schedule_truncates_one_cut_at_6x6_chi16():
+    """6x6, D = 4, chi = 16: each side truncates only the middle cut, after its
+    third row, so the result is the unique best rank-16 approximation there
+    (independent of the sweep order of the compression)."""
+    assert peps.chi_schedule(6, 6, 4, 16) == [[], [], [3]]
+    assert peps.chi_schedule(6, 6, 4, 64) == [[], [], []]
+    assert peps.chi_schedule(6, 6, 4, 8) == [[], [4, 3, 2], [4, 3, 2]]

@@ -1,0 +1,822 @@
+// Fermionic PEPS amplitudes with the reference's chi-truncated boundary
+// contraction (fPEPS_Model_GPU.amplitude / log_amplitude,
+// vmc_torch/GPU/models/pureTNS.py:81-146: contract_boundary_from_xmin_ over
+// rows [0, Lx/2-1] and contract_boundary_from_xmax_ over [Lx/2, Lx-1], both
+// with max_bond = chi and cutoff 0, then the two boundaries contracted).
+//
+// Formulation.  Each side's boundary is kept as the full vector over its
+// D^Ly open vertical legs (index sum_c d_c D^(Ly-1-c), column 0 most
+// significant).  A row is absorbed exactly, column by column, with the open
+// horizontal leg h as an extra index: W[h][idx], and per column c the 16
+// entries of every group (fixed other digits) map through the signed site
+// tensor A[h][old][h'][new] in place.  The boundary-MPS compression after a
+// row (left-to-right QR, then right-to-left SVD truncation to chi) is, in the
+// canonical sweep, the sequence of best rank-chi approximations of the whole
+// boundary state across cuts Ly-1, ..., 1; which cuts can exceed chi follows
+// from static bounds (a row multiplies a cut's bond by D, the rank never
+// exceeds min(D^k, D^(Ly-k)), truncating cut k bounds cut k-1 by D*chi), so
+// the host passes a per-row schedule of cuts and the others are skipped
+// (their truncation is the identity).  At 6x6, D = 4, chi = 16 each side
+// truncates only the middle cut, once.
+//
+// Truncation at cut k: the state as a matrix M (D^k x D^(Ly-k)); on its
+// smaller side the Gram matrix (M M^T or M^T M) is block-diagonal in the Z2
+// parity of the index (each tensor is parity-even), so two blocks of at most
+// 32 x 32.  One warp per block diagonalises it by cyclic Jacobi (pairs
+// (i, i xor m), m = 1..31: every pair once per sweep, 16 disjoint rotations a
+// round; lane i holds row i of the matrix and eigenvector i in registers; the
+// column half of each two-sided rotation goes through one transpose in shared
+// memory).  The chi largest eigenvalues over both blocks select the kept
+// eigenvectors U and the state becomes U U^T M.  This equals the SVD
+// truncation because the retained singular vectors are the Gram's top
+// eigenvectors; precision "fp64" runs everything in FP64, "fp32" the state,
+// Gram and Jacobi in FP32 with FP64 accumulation of the final overlap.
+//
+// After every absorbed row the state is rescaled by a power of two (exact)
+// and the exponent accumulated, so FP32 does not overflow.
+#include <climits>
+#include <type_traits>
+
+#include "common.cuh"
+#include "vmc_gb300.h"
+
+using namespace vmc;
+
+namespace {
+
+constexpr int CHI_NT = 256;
+constexpr int CHI_MAX_NS = 4096;      // D^Ly
+constexpr int CHI_MAX_ROWS = 32;      // rows per side
+constexpr int CHI_EXP_ZERO = INT_MIN, CHI_EXP_BAD = INT_MAX;
+
+struct ChiSched {
+  int Lx, Ly, D, NS, chi, rows;       // rows per side = Lx / 2
+  uint32_t cuts[CHI_MAX_ROWS];        // bit k: truncate cut k after this absorbed row
+};
+
+template <int D>
+__device__ __forceinline__ int digit_parity(uint32_t x) {
+  return D == 4 ? (__popc(x & 0x55555555u) & 1) : (__popc(x) & 1);
+}
+
+// small-side index of the i-th member of parity block b
+template <int D>
+__device__ __forceinline__ uint32_t block_member(int b, int i) {
+  const uint32_t e = (uint32_t)i << 1;
+  return e | (uint32_t)(b ^ digit_parity<D>(e));
+}
+
+template <typename T>
+struct ChiSmem {
+  // W: D * NS, A: D^4, S and V: 2 x 32 x 33 each, lam: 64, keep: 64 ints, red: 32
+  static size_t bytes(int NS, int D) {
+    return ((size_t)D * NS + (size_t)D * D * D * D + 4 * 32 * 33 + 64 + 32) * sizeof(T) + 64 * sizeof(int) + 16;
+  }
+};
+
+// One warp: eigen-decomposition of the symmetric 32 x 32 matrix in S (row
+// stride 33, zero-padded beyond nb) by cyclic Jacobi.  On return lam[i] holds
+// the eigenvalue of lane i and V[i * 33 + j] component j of its eigenvector.
+template <typename T>
+__device__ void warp_jacobi(T* S, T* V, T* lam) {
+  const int ln = threadIdx.x & 31;
+  T g[32], v[32];
+#pragma unroll
+  for (int j = 0; j < 32; ++j) {
+    g[j] = S[ln * 33 + j];
+    v[j] = (j == ln) ? T(1) : T(0);
+  }
+  const T tol = std::is_same<T, float>::value ? T(2e-7) : T(4e-16);
+  // rotations below tol * max|diag| are rounding noise of the largest entries
+  T floor_ = fabs(S[ln * 33 + ln]);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) floor_ = fmax(floor_, __shfl_xor_sync(VMC_FULL_MASK, floor_, o));
+  floor_ *= tol;
+  for (int sw = 0; sw < 20; ++sw) {
+    bool rotated = false;
+    for (int m = 1; m < 32; ++m) {
+      const int pr = ln ^ m;
+      const bool lead = ln < pr;
+      T c = T(1), s = T(0);
+      int need = 0;
+      if (lead) {
+        const T app = S[ln * 33 + ln], aqq = S[pr * 33 + pr], apq = S[ln * 33 + pr];
+        if (fabs(apq) > floor_ && fabs(apq) > tol * sqrt(fabs(app * aqq))) {
+          // Golub & Van Loan, sym.schur2: J = [[c, s], [-s, c]] zeroes (p, q) of J^T A J
+          const T tau = (aqq - app) / (T(2) * apq);
+          const T t = (tau >= T(0) ? T(1) : T(-1)) / (fabs(tau) + hypot(T(1), tau));
+          c = T(1) / sqrt(T(1) + t * t);
+          s = t * c;
+          need = 1;
+        }
+      }
+      const T c2 = __shfl_xor_sync(VMC_FULL_MASK, c, m), s2 = __shfl_xor_sync(VMC_FULL_MASK, s, m);
+      const int n2 = __shfl_xor_sync(VMC_FULL_MASK, need, m);
+      if (!lead) { c = c2; s = s2; need = n2; }
+      if (!__any_sync(VMC_FULL_MASK, need)) continue;
+      rotated = true;
+      // rows: H = J^T G
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {
+        const T o = __shfl_xor_sync(VMC_FULL_MASK, g[j], m);
+        g[j] = lead ? (c * g[j] - s * o) : (s * o + c * g[j]);
+      }
+      __syncwarp();
+#pragma unroll
+      for (int j = 0; j < 32; ++j) S[ln * 33 + j] = g[j];
+      __syncwarp();
+#pragma unroll
+      for (int j = 0; j < 32; ++j) g[j] = S[j * 33 + ln];
+      __syncwarp();
+      // rows of H^T = G J: J^T (G J) = G'
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {
+        const T o = __shfl_xor_sync(VMC_FULL_MASK, g[j], m);
+        g[j] = lead ? (c * g[j] - s * o) : (s * o + c * g[j]);
+      }
+#pragma unroll
+      for (int j = 0; j < 32; ++j) S[ln * 33 + j] = g[j];
+      __syncwarp();
+      // eigenvectors: V <- V J, lane i holds column i
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {
+        const T o = __shfl_xor_sync(VMC_FULL_MASK, v[j], m);
+        v[j] = lead ? (c * v[j] - s * o) : (s * o + c * v[j]);
+      }
+    }
+    if (!rotated) break;
+  }
+  lam[ln] = S[ln * 33 + ln];
+#pragma unroll
+  for (int j = 0; j < 32; ++j) V[ln * 33 + j] = v[j];
+  __syncwarp();
+}
+
+// Largest |x| of the CTA (thread 0's value is returned to every thread).
+template <typename T>
+__device__ T cta_absmax(T m, T* red) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(VMC_FULL_MASK, m, o));
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  T r = red[0];
+  for (int w = 1; w < (int)(blockDim.x >> 5); ++w) r = fmax(r, red[w]);
+  return r;
+}
+
+// Truncate the state psi = W[0 .. NS) to rank chi across the cut after k columns.
+template <typename T, int D>
+__device__ void chi_truncate(T* W, int NS, int Ly, int k, int chi, T* S, T* V, T* lam, int* keep) {
+  int nL = 1;
+  for (int i = 0; i < k; ++i) nL *= D;
+  const int nR = NS / nL;
+  const bool left = nL <= nR;
+  const int n = left ? nL : nR, nb = n >> 1, big = NS / n;
+  auto at = [&](uint32_t p, int q) -> int { return left ? (int)p * nR + q : q * nR + (int)p; };
+  T* Y = W + NS;  // the h = 1 slice is free between rows
+  // Gram blocks, zero-padded to 32 x 32
+  for (int e = threadIdx.x; e < 2 * 32 * 33; e += blockDim.x) S[e] = T(0);
+  __syncthreads();
+  const int tri = nb * (nb + 1) / 2;
+  for (int e = threadIdx.x; e < 2 * tri; e += blockDim.x) {
+    const int b = e / tri;
+    int r = e - b * tri, i = 0;
+    while (r > i) { r -= i + 1; ++i; }
+    const int j = r;
+    const uint32_t pi = block_member<D>(b, i), pj = block_member<D>(b, j);
+    T acc = T(0);
+    for (int q = 0; q < big; ++q) acc += W[at(pi, q)] * W[at(pj, q)];
+    S[b * 32 * 33 + i * 33 + j] = acc;
+    S[b * 32 * 33 + j * 33 + i] = acc;
+  }
+  __syncthreads();
+  const int warp = threadIdx.x >> 5;
+  if (warp < 2) warp_jacobi<T>(S + warp * 32 * 33, V + warp * 32 * 33, lam + warp * 32);
+  __syncthreads();
+  if (threadIdx.x < 64) {
+    const int b = threadIdx.x >> 5, i = threadIdx.x & 31;
+    int kp = 0;
+    if (i < nb) {
+      const T l = lam[b * 32 + i];
+      int rank = 0;
+      for (int e = 0; e < 64; ++e) {
+        const int b2 = e >> 5, i2 = e & 31;
+        if (i2 >= nb) continue;
+        const T l2 = lam[e];
+        rank += (l2 > l) || (l2 == l && (b2 < b || (b2 == b && i2 < i)));
+      }
+      kp = rank < chi;
+    }
+    keep[threadIdx.x] = kp;
+  }
+  __syncthreads();
+  // Y[b][i][q] = v_i . psi_b(:, q) for kept i
+  for (int e = threadIdx.x; e < NS; e += blockDim.x) {
+    const int bi = e / big, q = e - bi * big, b = bi / nb, i = bi - b * nb;
+    T acc = T(0);
+    if (keep[b * 32 + i]) {
+      const T* vi = V + b * 32 * 33 + i * 33;
+      for (int j = 0; j < nb; ++j) acc += vi[j] * W[at(block_member<D>(b, j), q)];
+    }
+    Y[e] = acc;
+  }
+  __syncthreads();
+  // psi_b(p_j, q) = sum_i v_i[j] Y[b][i][q]
+  for (int e = threadIdx.x; e < NS; e += blockDim.x) {
+    const int bj = e / big, q = e - bj * big, b = bj / nb, j = bj - b * nb;
+    T acc = T(0);
+    for (int i = 0; i < nb; ++i)
+      if (keep[b * 32 + i]) acc += V[b * 32 * 33 + i * 33 + j] * Y[(b * nb + i) * big + q];
+    W[at(block_member<D>(b, j), q)] = acc;
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < NS; e += blockDim.x) Y[e] = T(0);
+  __syncthreads();
+}
+
+// Boundary state of one side for one configuration.  item -> configuration
+// cfg[2 * ci], side (0 = top rows [0, Lx/2), 1 = bottom rows [Lx/2, Lx)):
+// sides == nullptr: ci = item >> 1, side = item & 1; else ci = cfg_idx[item]
+// (or item when cfg_idx is null), side = sides[item].  The state goes to slot
+// 2 * ci + side of out / expo_out.  count: optional device item count (items
+// past it exit).
+template <typename T, int D>
+__global__ void __launch_bounds__(CHI_NT)
+    k_chi_side(const T* __restrict__ tens, ChiSched sc, const uint64_t* __restrict__ cfg,
+               const int32_t* __restrict__ cfg_idx, const uint8_t* __restrict__ sides, int64_t n_items,
+               const int* __restrict__ count, T* __restrict__ out, int* __restrict__ expo_out) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int64_t item = blockIdx.x;
+  if (item >= n_items || (count && item >= *count)) return;
+  const int NS = sc.NS, Ly = sc.Ly, Lx = sc.Lx;
+  T* W = reinterpret_cast<T*>(smraw);
+  T* A = W + (size_t)D * NS;
+  T* S = A + D * D * D * D;
+  T* V = S + 2 * 32 * 33;
+  T* lam = V + 2 * 32 * 33;
+  T* red = lam + 64;
+  int* keep = reinterpret_cast<int*>(red + 32);
+  int64_t ci;
+  int side;
+  if (sides) { ci = cfg_idx ? cfg_idx[item] : item; side = sides[item]; }
+  else { ci = item >> 1; side = (int)(item & 1); }
+  const uint64_t up = cfg[2 * ci], dn = cfg[2 * ci + 1];
+  for (int e = threadIdx.x; e < D * NS; e += blockDim.x) W[e] = (e == 0) ? T(1) : T(0);
+  int expo = 0;
+  bool zero = false, bad = false;
+  for (int a = 0; a < sc.rows && !zero && !bad; ++a) {
+    const int r = side ? (Lx - 1 - a) : a;
+    int nleft = 0;
+    int stride = NS / D;
+    for (int c = 0; c < Ly; ++c, stride /= D) {
+      const int site = r * Ly + c;
+      const int x = site_state(up, dn, site);
+      __syncthreads();
+      const T* ts = tens + ((size_t)site * 4 + x) * (D * D * D * D);
+      for (int e = threadIdx.x; e < D * D * D * D; e += blockDim.x) {
+        const int n = e % D, hp = (e / D) % D, o = (e / (D * D)) % D, h = e / (D * D * D);
+        const int u = side ? n : o, d = side ? o : n;
+        T val = ts[((h * D + u) * D + hp) * D + d];
+        if (r >= 1 && (u & 1) && ((h + nleft) & 1)) val = -val;
+        A[e] = val;
+      }
+      __syncthreads();
+      for (int gi = threadIdx.x; gi < NS / D; gi += blockDim.x) {
+        const int lo = gi % stride, hi = gi / stride;
+        const int base = hi * stride * D + lo;
+        T in[D][D];
+        bool any = false;
+#pragma unroll
+        for (int o = 0; o < D; ++o)
+#pragma unroll
+          for (int hh = 0; hh < D; ++hh) {
+            in[o][hh] = W[hh * NS + base + o * stride];
+            any |= in[o][hh] != T(0);
+          }
+        if (!any) continue;
+        T outv[D][D];
+#pragma unroll
+        for (int nn = 0; nn < D; ++nn)
+#pragma unroll
+          for (int hp = 0; hp < D; ++hp) outv[nn][hp] = T(0);
+#pragma unroll
+        for (int hh = 0; hh < D; ++hh)
+#pragma unroll
+          for (int o = 0; o < D; ++o) {
+            const T a0 = in[o][hh];
+            const T* Ar = A + (hh * D + o) * D * D;
+#pragma unroll
+            for (int hp = 0; hp < D; ++hp)
+#pragma unroll
+              for (int nn = 0; nn < D; ++nn) outv[nn][hp] += a0 * Ar[hp * D + nn];
+          }
+#pragma unroll
+        for (int nn = 0; nn < D; ++nn)
+#pragma unroll
+          for (int hp = 0; hp < D; ++hp) W[hp * NS + base + nn * stride] = outv[nn][hp];
+      }
+      nleft += __popcll((up >> site) & 1ull) + __popcll((dn >> site) & 1ull);
+    }
+    __syncthreads();
+    // rescale the state (the h != 0 slices are zero after the open right edge)
+    T m = T(0);
+    int nonfinite = 0;
+    for (int e = threadIdx.x; e < NS; e += blockDim.x) {
+      const T x = fabs(W[e]);
+      nonfinite |= !(x < T(INFINITY));
+      m = fmax(m, x);
+    }
+    if (__syncthreads_or(nonfinite)) { bad = true; break; }
+    m = cta_absmax<T>(m, red);
+    if (m == T(0)) { zero = true; break; }
+    const int e2 = (int)ilogb(m);
+    expo += e2;
+    __syncthreads();
+    for (int e = threadIdx.x; e < NS; e += blockDim.x) W[e] = scalbn(W[e], -e2);
+    __syncthreads();
+    for (int k = Ly - 1; k >= 1; --k)
+      if ((sc.cuts[a] >> k) & 1u) chi_truncate<T, D>(W, NS, Ly, k, sc.chi, S, V, lam, keep);
+  }
+  __syncthreads();
+  const int64_t slot = sides ? 2 * ci + side : item;
+  T* dst = out + slot * (int64_t)NS;
+  for (int e = threadIdx.x; e < NS; e += blockDim.x) dst[e] = (zero || bad) ? T(0) : W[e];
+  if (threadIdx.x == 0) expo_out[slot] = bad ? CHI_EXP_BAD : (zero ? CHI_EXP_ZERO : expo);
+}
+
+// (sign, log|psi|) from <top, bottom> * 2^(et + eb) and the global sign.
+__device__ __forceinline__ void chi_finish(double v, int et, int eb, uint64_t up, uint64_t dn, double& sgn,
+                                           double& la) {
+  const int K = __popcll(up ^ dn);
+  const double g = ((K * (K - 1) / 2) & 1) ? -1.0 : 1.0;
+  if (et == CHI_EXP_BAD || eb == CHI_EXP_BAD || !isfinite(v)) { sgn = 0.0; la = NAN; }
+  else if (et == CHI_EXP_ZERO || eb == CHI_EXP_ZERO || v == 0.0) { sgn = 0.0; la = -INFINITY; }
+  else {
+    sgn = v < 0 ? -g : g;
+    la = log(fabs(v)) + (double)(et + eb) * 0.69314718055994530942;
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ double warp_dot(const T* a, const T* b, int NS) {
+  double acc = 0.0;
+  for (int e = threadIdx.x & 31; e < NS; e += 32) acc += (double)a[e] * (double)b[e];
+  return warp_sum(acc);
+}
+
+// One warp per configuration: states at st[(2w) * NS] (top), st[(2w+1) * NS].
+template <typename T>
+__global__ void k_chi_dot(const T* __restrict__ st, const int* __restrict__ ex, int NS,
+                          const uint64_t* __restrict__ occ, int64_t R, double* __restrict__ sign,
+                          double* __restrict__ logabs) {
+  const int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (w >= R) return;
+  const double v = warp_dot(st + 2 * w * NS, st + (2 * w + 1) * NS, NS);
+  if ((threadIdx.x & 31) == 0) {
+    double s, la;
+    chi_finish(v, ex[2 * w], ex[2 * w + 1], occ[2 * w], occ[2 * w + 1], s, la);
+    sign[w] = s;
+    logabs[w] = la;
+  }
+}
+
+
+// Warp-aggregated append of k items (k in {0, 1, 2}) to a device list; returns
+// the first index of this lane's items.
+__device__ __forceinline__ int warp_append(int k, int* count) {
+  const int ln = threadIdx.x & 31;
+  int incl = k;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(VMC_FULL_MASK, incl, o);
+    if (ln >= o) incl += y;
+  }
+  const int tot = __shfl_sync(VMC_FULL_MASK, incl, 31);
+  int base = 0;
+  if (ln == 31 && tot) base = atomicAdd(count, tot);
+  base = __shfl_sync(VMC_FULL_MASK, base, 31);
+  return base + incl - k;
+}
+
+// Sides whose boundary state a change of sites i and j touches.
+__device__ __forceinline__ int touched_sides(int i, int j, int Ly, int half) {
+  const int ri = i / Ly, rj = j / Ly;
+  return ((ri < half || rj < half) ? 1 : 0) | ((ri >= half || rj >= half) ? 2 : 0);
+}
+
+// One proposal per walker on edge e (the draws and proposal of k_peps_sweep):
+// proposed configuration, touched sides, and the side-state items to build.
+__global__ void k_chi_propose(const uint64_t* __restrict__ occ, int64_t n, int64_t w0, int64_t B, int Ly, int half,
+                              const int32_t* __restrict__ edges, int e, int E, int s, float hopping_rate,
+                              uint64_t seed, uint64_t sweep_offset, const float* __restrict__ r_move,
+                              const uint8_t* __restrict__ r_bit, const float* __restrict__ r_acc,
+                              uint64_t* __restrict__ prop, uint8_t* __restrict__ flags, float* __restrict__ u_acc,
+                              int32_t* __restrict__ cfg_idx, uint8_t* __restrict__ sides, int* __restrict__ count) {
+  const int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int f = 0;
+  if (w < n) {
+    const uint64_t up = occ[2 * w], dn = occ[2 * w + 1];
+    const int i = edges[2 * e], j = edges[2 * e + 1];
+    const int xi = site_state(up, dn, i), xj = site_state(up, dn, j);
+    if (xi != xj) {
+      float um, ua;
+      int bit;
+      const int64_t gw = w0 + w;
+      if (r_move) {
+        const size_t ridx = ((size_t)s * E + e) * (size_t)B + (size_t)gw;
+        um = r_move[ridx]; bit = r_bit[ridx] & 1; ua = r_acc[ridx];
+      } else {
+        EdgeDraw d = draw_edge(seed, (uint64_t)gw, sweep_offset + (uint64_t)s, (uint32_t)e);
+        um = d.u_move; bit = d.bit; ua = d.u_acc;
+      }
+      int ni, nj;
+      propose_pair(xi, xj, um, bit, hopping_rate, ni, nj);
+      const uint64_t mi = 1ull << i, mj = 1ull << j;
+      uint64_t up1 = up & ~(mi | mj), dn1 = dn & ~(mi | mj);
+      if (ni & 2) up1 |= mi;
+      if (ni & 1) dn1 |= mi;
+      if (nj & 2) up1 |= mj;
+      if (nj & 1) dn1 |= mj;
+      prop[2 * w] = up1;
+      prop[2 * w + 1] = dn1;
+      u_acc[w] = ua;
+      f = touched_sides(i, j, Ly, half);
+    }
+    flags[w] = (uint8_t)f;
+  }
+  const int k = (f & 1) + ((f >> 1) & 1);
+  const int base = warp_append(k, count);
+  int o = base;
+  if (f & 1) { cfg_idx[o] = (int32_t)w; sides[o] = 0; ++o; }
+  if (f & 2) { cfg_idx[o] = (int32_t)w; sides[o] = 1; }
+}
+
+// Metropolis decision for every walker with a proposal: amplitude from the
+// rebuilt sides (new) and the kept ones (cur); on acceptance the new states
+// replace the current ones.  One warp per walker.
+template <typename T>
+__global__ void k_chi_accept(int NS, int64_t n, T* __restrict__ cur, int* __restrict__ cur_ex,
+                             const T* __restrict__ nw, const int* __restrict__ nw_ex, const uint8_t* __restrict__ flags,
+                             const uint64_t* __restrict__ prop, const float* __restrict__ u_acc,
+                             uint64_t* __restrict__ occ, double* __restrict__ sign, double* __restrict__ logabs,
+                             int32_t* __restrict__ n_acc, unsigned long long* __restrict__ n_eval) {
+  __shared__ int evals, builds;
+  if (threadIdx.x == 0) { evals = 0; builds = 0; }
+  __syncthreads();
+  const int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int ln = threadIdx.x & 31;
+  const int f = (w < n) ? flags[w] : 0;
+  if (f) {
+    const T* a = ((f & 1) ? nw : cur) + 2 * w * NS;
+    const T* b = ((f & 2) ? nw : cur) + (2 * w + 1) * NS;
+    const int et = ((f & 1) ? nw_ex : cur_ex)[2 * w], eb = ((f & 2) ? nw_ex : cur_ex)[2 * w + 1];
+    const double v = warp_dot(a, b, NS);
+    int acc = 0;
+    double s1 = 0.0, la1 = 0.0;
+    if (ln == 0) {
+      chi_finish(v, et, eb, prop[2 * w], prop[2 * w + 1], s1, la1);
+      const double la = logabs[w];
+      if (!(la1 > -INFINITY)) acc = 0;
+      else if (la == -INFINITY) acc = 1;
+      else acc = (double)u_acc[w] < exp(2.0 * (la1 - la));
+      atomicAdd(&evals, 1);
+      atomicAdd(&builds, (f & 1) + ((f >> 1) & 1));
+    }
+    acc = __shfl_sync(VMC_FULL_MASK, acc, 0);
+    if (acc) {
+      for (int sd = 0; sd < 2; ++sd)
+        if (f & (1 << sd)) {
+          const int64_t o = (2 * w + sd) * NS;
+          for (int e2 = ln; e2 < NS; e2 += 32) cur[o + e2] = nw[o + e2];
+          if (ln == 0) cur_ex[2 * w + sd] = nw_ex[2 * w + sd];
+        }
+      if (ln == 0) {
+        occ[2 * w] = prop[2 * w];
+        occ[2 * w + 1] = prop[2 * w + 1];
+        sign[w] = s1;
+        logabs[w] = la1;
+        if (n_acc) n_acc[w] += 1;
+      }
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && n_eval && evals) {
+    atomicAdd(n_eval, (unsigned long long)evals);
+    atomicAdd(n_eval + 1, (unsigned long long)builds);
+  }
+}
+
+// Local-energy terms: the configuration of every hop term (the move of
+// k_peps_conn_terms) and the side states it needs rebuilt.
+__global__ void k_chi_term_prep(const uint64_t* __restrict__ occ, int N, int Ly, int half,
+                                const int32_t* __restrict__ pairs, int64_t p0, int64_t np, int64_t w0,
+                                const int32_t* __restrict__ edges, uint64_t* __restrict__ prop,
+                                uint8_t* __restrict__ flags, int32_t* __restrict__ cfg_idx,
+                                uint8_t* __restrict__ sides, int* __restrict__ count) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int f = 0;
+  if (p < np) {
+    const int w = pairs[2 * (p0 + p)], tm = pairs[2 * (p0 + p) + 1];
+    const uint64_t up = occ[2 * (int64_t)w], dn = occ[2 * (int64_t)w + 1];
+    const int e = tm >> 1, sp = (tm & 1) ? 0 : 1;
+    int i = edges[2 * e], j = edges[2 * e + 1];
+    if (i > j) { const int tt = i; i = j; j = tt; }
+    const uint64_t m = sp ? up : dn;
+    const int oi = (int)((m >> i) & 1ull);
+    const int base = sp ? 0 : N;
+    uint64_t eu = up, ed = dn;
+    apply_move(eu, ed, N, base + (oi ? i : j), base + (oi ? j : i));
+    prop[2 * p] = eu;
+    prop[2 * p + 1] = ed;
+    f = touched_sides(i, j, Ly, half);
+    flags[p] = (uint8_t)f;
+    (void)w0;
+  }
+  const int k = (f & 1) + ((f >> 1) & 1);
+  const int b = warp_append(k, count);
+  int o = b;
+  if (f & 1) { cfg_idx[o] = (int32_t)p; sides[o] = 0; ++o; }
+  if (f & 2) { cfg_idx[o] = (int32_t)p; sides[o] = 1; }
+}
+
+// term = H_{x,x'} psi(x') / psi(x) for each pair of the block; the walker's
+// own states (cur, slot 2(w - w0) + side) fill in the untouched side.
+template <typename T>
+__global__ void k_chi_terms(int NS, int N, const uint64_t* __restrict__ occ, const int32_t* __restrict__ pairs,
+                            int64_t p0, int64_t np, int64_t w0, const int32_t* __restrict__ edges, double t,
+                            const T* __restrict__ cur, const int* __restrict__ cur_ex, const double* __restrict__ s0a,
+                            const double* __restrict__ la0a, const T* __restrict__ nw, const int* __restrict__ nw_ex,
+                            const uint8_t* __restrict__ flags, const uint64_t* __restrict__ prop,
+                            double* __restrict__ term) {
+  const int64_t p = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (p >= np) return;
+  const int w = pairs[2 * (p0 + p)], tm = pairs[2 * (p0 + p) + 1];
+  const int64_t lw = w - w0;
+  const int f = flags[p];
+  const T* a = (f & 1) ? nw + 2 * p * NS : cur + 2 * lw * NS;
+  const T* b = (f & 2) ? nw + (2 * p + 1) * NS : cur + (2 * lw + 1) * NS;
+  const int et = (f & 1) ? nw_ex[2 * p] : cur_ex[2 * lw], eb = (f & 2) ? nw_ex[2 * p + 1] : cur_ex[2 * lw + 1];
+  const double v = warp_dot(a, b, NS);
+  if ((threadIdx.x & 31) == 0) {
+    const uint64_t up = occ[2 * (int64_t)w], dn = occ[2 * (int64_t)w + 1];
+    const int e = tm >> 1, sp = (tm & 1) ? 0 : 1;
+    int i = edges[2 * e], j = edges[2 * e + 1];
+    if (i > j) { const int tt = i; i = j; j = tt; }
+    const double coeff = symmray_parity(up, dn, i, j, sp) ? t : -t;
+    double s1, la1;
+    chi_finish(v, et, eb, prop[2 * p], prop[2 * p + 1], s1, la1);
+    const double s0 = s0a[lw], la0 = la0a[lw];
+    term[p0 + p] = (s1 == 0.0 || s0 == 0.0) ? 0.0 : coeff * s1 * s0 * exp(la1 - la0);
+    (void)N;
+  }
+}
+
+__global__ void k_chi_eloc_reduce(int64_t B, const uint64_t* __restrict__ occ, const int32_t* __restrict__ offs,
+                                  const double* __restrict__ term, double U, double* __restrict__ eloc) {
+  const int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= B) return;
+  double s = U * (double)__popcll(occ[2 * w] & occ[2 * w + 1]);
+  for (int q = offs[w]; q < offs[w + 1]; ++q) s += term[q];
+  eloc[w] = s;
+}
+
+int chi_plan(int Lx, int Ly, int D, int chi, ChiSched& sc) {
+  if (Lx < 2 || (Lx & 1) || Ly < 1 || Lx * Ly > 64 || (D != 2 && D != 4) || chi < 1) return VMC_ERR_UNSUPPORTED;
+  int64_t NS = 1;
+  for (int c = 0; c < Ly; ++c) NS *= D;
+  if (NS > CHI_MAX_NS || NS < 2) return VMC_ERR_UNSUPPORTED;
+  sc = ChiSched{};
+  sc.Lx = Lx; sc.Ly = Ly; sc.D = D; sc.NS = (int)NS; sc.chi = chi; sc.rows = Lx / 2;
+  int64_t b[16];
+  for (int k = 0; k <= Ly; ++k) b[k] = 1;
+  for (int a = 0; a < sc.rows; ++a) {
+    for (int k = 1; k < Ly; ++k) {
+      int64_t lk = 1, rk = 1;
+      for (int i = 0; i < k; ++i) lk *= D;
+      for (int i = k; i < Ly; ++i) rk *= D;
+      int64_t nb = b[k] * D;
+      if (nb > lk) nb = lk;
+      if (nb > rk) nb = rk;
+      b[k] = nb;
+    }
+    uint32_t m = 0;
+    if (a >= 1)
+      for (int k = Ly - 1; k >= 1; --k)
+        if (b[k] > chi) {
+          m |= 1u << k;
+          b[k] = chi;
+          if (k > 1 && b[k - 1] > (int64_t)D * chi) b[k - 1] = (int64_t)D * chi;
+        }
+    sc.cuts[a] = m;
+  }
+  return VMC_OK;
+}
+
+template <typename T>
+int launch_chi_side(const void* tens, const ChiSched& sc, const uint64_t* cfg, const int32_t* cfg_idx,
+                    const uint8_t* sides, int64_t n_items, const int* count, T* out, int* ex, cudaStream_t st) {
+  if (n_items <= 0) return VMC_OK;
+  const size_t smem = ChiSmem<T>::bytes(sc.NS, sc.D);
+  if (sc.D == 4) {
+    if (cudaFuncSetAttribute(k_chi_side<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+      return VMC_ERR_CUDA;
+    k_chi_side<T, 4><<<(unsigned)n_items, CHI_NT, smem, st>>>((const T*)tens, sc, cfg, cfg_idx, sides, n_items,
+                                                               count, out, ex);
+  } else {
+    if (cudaFuncSetAttribute(k_chi_side<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+      return VMC_ERR_CUDA;
+    k_chi_side<T, 2><<<(unsigned)n_items, CHI_NT, smem, st>>>((const T*)tens, sc, cfg, cfg_idx, sides, n_items,
+                                                               count, out, ex);
+  }
+  VMC_CUDA_CHECK_LAUNCH();
+  return VMC_OK;
+}
+
+
+// Per-chunk workspace (work_rows walkers): current and new side states, their
+// exponents, proposed configurations, item lists.
+template <typename T>
+struct ChiWork {
+  T* cur; T* nw; int* cur_ex; int* nw_ex; uint64_t* prop; int32_t* cfg_idx; uint8_t* sides; uint8_t* flags;
+  float* u_acc; int* count; double* s0; double* la0;
+  static int64_t bytes(int NS, int64_t rows) {
+    return rows * (4 * (int64_t)NS * (int64_t)sizeof(T) + 4 * 4 + 16 + 8 + 2 + 1 + 4 + 16) + 16 * 256;
+  }
+  ChiWork(void* base, int NS, int64_t rows) {
+    char* p = (char*)base;
+    auto take = [&](int64_t nbytes) { char* q = p; p += (nbytes + 255) & ~int64_t(255); return q; };
+    cur = (T*)take(2 * rows * NS * (int64_t)sizeof(T));
+    nw = (T*)take(2 * rows * NS * (int64_t)sizeof(T));
+    prop = (uint64_t*)take(2 * rows * 8);
+    s0 = (double*)take(rows * 8);
+    la0 = (double*)take(rows * 8);
+    cur_ex = (int*)take(2 * rows * 4);
+    nw_ex = (int*)take(2 * rows * 4);
+    cfg_idx = (int32_t*)take(2 * rows * 4);
+    u_acc = (float*)take(rows * 4);
+    count = (int*)take(256);
+    sides = (uint8_t*)take(2 * rows);
+    flags = (uint8_t*)take(rows);
+  }
+};
+
+template <typename T>
+int chi_eval(const void* tens, const ChiSched& sc, const uint64_t* occ, int64_t R, double* sign, double* logabs,
+             void* work, int64_t work_rows, cudaStream_t st) {
+  ChiWork<T> W(work, sc.NS, work_rows);
+  for (int64_t w0 = 0; w0 < R; w0 += work_rows) {
+    const int64_t n = (R - w0) < work_rows ? (R - w0) : work_rows;
+    int rc = launch_chi_side<T>(tens, sc, occ + 2 * w0, nullptr, nullptr, 2 * n, nullptr, W.cur, W.cur_ex, st);
+    if (rc) return rc;
+    k_chi_dot<T><<<(unsigned)((n + 7) / 8), 256, 0, st>>>(W.cur, W.cur_ex, sc.NS, occ + 2 * w0, n, sign + w0,
+                                                          logabs + w0);
+    VMC_CUDA_CHECK_LAUNCH();
+  }
+  return VMC_OK;
+}
+
+template <typename T>
+int chi_sweep(const void* tens, const ChiSched& sc, uint64_t* occ, int64_t B, const int32_t* edges, int E,
+              int n_sweeps, float hopping_rate, uint64_t seed, uint64_t sweep_offset, const float* r_move,
+              const uint8_t* r_bit, const float* r_acc, double* sign, double* logabs, int32_t* n_acc,
+              unsigned long long* n_eval, void* work, int64_t work_rows, cudaStream_t st) {
+  ChiWork<T> W(work, sc.NS, work_rows);
+  for (int64_t w0 = 0; w0 < B; w0 += work_rows) {
+    const int64_t n = (B - w0) < work_rows ? (B - w0) : work_rows;
+    int rc = launch_chi_side<T>(tens, sc, occ + 2 * w0, nullptr, nullptr, 2 * n, nullptr, W.cur, W.cur_ex, st);
+    if (rc) return rc;
+    k_chi_dot<T><<<(unsigned)((n + 7) / 8), 256, 0, st>>>(W.cur, W.cur_ex, sc.NS, occ + 2 * w0, n, sign + w0,
+                                                          logabs + w0);
+    VMC_CUDA_CHECK_LAUNCH();
+    for (int s = 0; s < n_sweeps; ++s)
+      for (int e = 0; e < E; ++e) {
+        if (cudaMemsetAsync(W.count, 0, sizeof(int), st) != cudaSuccess) return VMC_ERR_CUDA;
+        k_chi_propose<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
+            occ + 2 * w0, n, w0, B, sc.Ly, sc.rows, edges, e, E, s, hopping_rate, seed, sweep_offset, r_move, r_bit,
+            r_acc, W.prop, W.flags, W.u_acc, W.cfg_idx, W.sides, W.count);
+        VMC_CUDA_CHECK_LAUNCH();
+        rc = launch_chi_side<T>(tens, sc, W.prop, W.cfg_idx, W.sides, 2 * n, W.count, W.nw, W.nw_ex, st);
+        if (rc) return rc;
+        k_chi_accept<T><<<(unsigned)((n + 7) / 8), 256, 0, st>>>(sc.NS, n, W.cur, W.cur_ex, W.nw, W.nw_ex, W.flags,
+                                                                 W.prop, W.u_acc, occ + 2 * w0, sign + w0,
+                                                                 logabs + w0, n_acc ? n_acc + w0 : nullptr, n_eval);
+        VMC_CUDA_CHECK_LAUNCH();
+      }
+  }
+  return VMC_OK;
+}
+
+// The pair range of a walker chunk comes from offs_host (a host copy of offs).
+template <typename T>
+int chi_local_energy(const void* tens, const ChiSched& sc, const uint64_t* occ, int64_t B, const int32_t* edges,
+                     double t, double U, const int32_t* pairs, const int32_t* offs, const int32_t* offs_host,
+                     double* term, double* eloc, void* work, int64_t work_rows, cudaStream_t st) {
+  ChiWork<T> W(work, sc.NS, work_rows);
+  const int N = sc.Lx * sc.Ly;
+  for (int64_t w0 = 0; w0 < B; w0 += work_rows) {
+    const int64_t n = (B - w0) < work_rows ? (B - w0) : work_rows;
+    int rc = launch_chi_side<T>(tens, sc, occ + 2 * w0, nullptr, nullptr, 2 * n, nullptr, W.cur, W.cur_ex, st);
+    if (rc) return rc;
+    k_chi_dot<T><<<(unsigned)((n + 7) / 8), 256, 0, st>>>(W.cur, W.cur_ex, sc.NS, occ + 2 * w0, n, W.s0, W.la0);
+    VMC_CUDA_CHECK_LAUNCH();
+    const int64_t pa = offs_host[w0], pb = offs_host[w0 + n];
+    for (int64_t p0 = pa; p0 < pb; p0 += work_rows) {
+      const int64_t np = (pb - p0) < work_rows ? (pb - p0) : work_rows;
+      if (cudaMemsetAsync(W.count, 0, sizeof(int), st) != cudaSuccess) return VMC_ERR_CUDA;
+      k_chi_term_prep<<<(unsigned)((np + 255) / 256), 256, 0, st>>>(occ, N, sc.Ly, sc.rows, pairs, p0, np, w0, edges,
+                                                                    W.prop, W.flags, W.cfg_idx, W.sides, W.count);
+      VMC_CUDA_CHECK_LAUNCH();
+      rc = launch_chi_side<T>(tens, sc, W.prop, W.cfg_idx, W.sides, 2 * np, W.count, W.nw, W.nw_ex, st);
+      if (rc) return rc;
+      k_chi_terms<T><<<(unsigned)((np + 7) / 8), 256, 0, st>>>(sc.NS, N, occ, pairs, p0, np, w0, edges, t, W.cur,
+                                                               W.cur_ex, W.s0, W.la0, W.nw, W.nw_ex, W.flags, W.prop,
+                                                               term);
+      VMC_CUDA_CHECK_LAUNCH();
+    }
+  }
+  k_chi_eloc_reduce<<<(unsigned)((B + 255) / 256), 256, 0, st>>>(B, occ, offs, term, U, eloc);
+  VMC_CUDA_CHECK_LAUNCH();
+  return VMC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int vmc_peps_chi_work_bytes(int prec, int Lx, int Ly, int D, int chi, int64_t work_rows, int64_t* bytes) {
+  ChiSched sc;
+  if ((prec != 0 && prec != 1) || work_rows <= 0 || !bytes) return VMC_ERR_ARGS;
+  int rc = chi_plan(Lx, Ly, D, chi, sc);
+  if (rc) return rc;
+  *bytes = prec == 0 ? ChiWork<float>::bytes(sc.NS, work_rows) : ChiWork<double>::bytes(sc.NS, work_rows);
+  return VMC_OK;
+}
+
+int vmc_peps_chi_schedule(int Lx, int Ly, int D, int chi, uint32_t* cuts, int max_rows) {
+  ChiSched sc;
+  int rc = chi_plan(Lx, Ly, D, chi, sc);
+  if (rc) return rc;
+  if (!cuts || max_rows < sc.rows) return VMC_ERR_ARGS;
+  for (int a = 0; a < sc.rows; ++a) cuts[a] = sc.cuts[a];
+  return VMC_OK;
+}
+
+int vmc_peps_chi_eval(int prec, const void* tensors, int Lx, int Ly, int D, int chi, const uint64_t* occ, int64_t R,
+                      double* sign, double* logabs, void* work, int64_t work_rows, void* stream) {
+  ChiSched sc;
+  if (prec != 0 && prec != 1) return VMC_ERR_ARGS;
+  int rc = chi_plan(Lx, Ly, D, chi, sc);
+  if (rc) return rc;
+  if (R < 0 || work_rows <= 0) return VMC_ERR_ARGS;
+  if (R == 0) return VMC_OK;
+  if (!tensors || !occ || !sign || !logabs || !work) return VMC_ERR_ARGS;
+  cudaStream_t st = (cudaStream_t)stream;
+  return prec == 0 ? chi_eval<float>(tensors, sc, occ, R, sign, logabs, work, work_rows, st)
+                   : chi_eval<double>(tensors, sc, occ, R, sign, logabs, work, work_rows, st);
+}
+
+int vmc_peps_chi_sweep(int prec, const void* tensors, int Lx, int Ly, int D, int chi, uint64_t* occ, int64_t B,
+                       const int32_t* edges, int n_edges, int n_sweeps, float hopping_rate, uint64_t seed,
+                       uint64_t sweep_offset, const float* r_move, const uint8_t* r_bit, const float* r_acc,
+                       double* sign, double* logabs, int32_t* n_acc, uint64_t* d_n_eval, void* work,
+                       int64_t work_rows, void* stream) {
+  ChiSched sc;
+  if (prec != 0 && prec != 1) return VMC_ERR_ARGS;
+  int rc = chi_plan(Lx, Ly, D, chi, sc);
+  if (rc) return rc;
+  if (B < 0 || n_edges < 0 || n_sweeps < 0 || work_rows <= 0) return VMC_ERR_ARGS;
+  if ((r_move != nullptr) != (r_acc != nullptr) || (r_move != nullptr) != (r_bit != nullptr)) return VMC_ERR_ARGS;
+  if (B == 0) return VMC_OK;
+  if (!tensors || !occ || !sign || !logabs || !work || (n_edges > 0 && !edges)) return VMC_ERR_ARGS;
+  if (B > INT32_MAX || work_rows > (INT32_MAX / 2)) return VMC_ERR_ARGS;
+  cudaStream_t st = (cudaStream_t)stream;
+  unsigned long long* ne = (unsigned long long*)d_n_eval;
+  return prec == 0 ? chi_sweep<float>(tensors, sc, occ, B, edges, n_edges, n_sweeps, hopping_rate, seed,
+                                      sweep_offset, r_move, r_bit, r_acc, sign, logabs, n_acc, ne, work, work_rows, st)
+                   : chi_sweep<double>(tensors, sc, occ, B, edges, n_edges, n_sweeps, hopping_rate, seed,
+                                       sweep_offset, r_move, r_bit, r_acc, sign, logabs, n_acc, ne, work, work_rows,
+                                       st);
+}
+
+int vmc_peps_chi_local_energy(int prec, const void* tensors, int Lx, int Ly, int D, int chi, const uint64_t* occ,
+                              int64_t B, const int32_t* edges, double t, double U, const int32_t* pairs,
+                              const int32_t* offs, const int32_t* offs_host, int64_t P, double* term, double* eloc,
+                              void* work, int64_t work_rows, void* stream) {
+  ChiSched sc;
+  if (prec != 0 && prec != 1) return VMC_ERR_ARGS;
+  int rc = chi_plan(Lx, Ly, D, chi, sc);
+  if (rc) return rc;
+  if (B < 0 || P < 0 || work_rows <= 0) return VMC_ERR_ARGS;
+  if (B == 0) return VMC_OK;
+  if (!tensors || !occ || !offs || !offs_host || !eloc || !work || (P > 0 && (!pairs || !edges || !term)))
+    return VMC_ERR_ARGS;
+  if (offs_host[0] != 0 || offs_host[B] != P || work_rows > (INT32_MAX / 2)) return VMC_ERR_ARGS;
+  cudaStream_t st = (cudaStream_t)stream;
+  return prec == 0 ? chi_local_energy<float>(tensors, sc, occ, B, edges, t, U, pairs, offs, offs_host, term, eloc,
+                                             work, work_rows, st)
+                   : chi_local_energy<double>(tensors, sc, occ, B, edges, t, U, pairs, offs, offs_host, term, eloc,
+                                              work, work_rows, st);
+}
+
+}  // extern "C"

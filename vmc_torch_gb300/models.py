@@ -584,13 +584,17 @@ class FPEPS_GB300(WavefunctionModel_GB300):
     zero).  Sites are numbered ``row * Ly + col`` like the Hamiltonian's.
 
     The amplitude is the Grassmann contraction of the network (bond variables
-    ordered left, up, down, right within a site), evaluated exactly by the
-    kernels: top/bottom boundary MPSs of bond D^(Lx/2-1) and a column sweep
-    through the two middle rows.  The reference contracts boundary MPSs
-    truncated to ``max_bond`` with SVDs (pureTNS.py:103-114); for
-    ``max_bond >= D**(Lx//2)`` that truncation is exact and the two agree.
-    ``max_bond`` is accepted for interface compatibility; the contraction here
-    is always the exact (max_bond -> infinity) one.
+    ordered left, up, down, right within a site) with the reference's
+    boundary contraction (pureTNS.py:100-111): rows [0, Lx/2) absorbed from the
+    top and rows [Lx/2, Lx) from the bottom into boundaries truncated to
+    ``max_bond`` = chi after every row (cutoff 0), then contracted.  When no cut
+    can exceed chi (``max_bond`` None or <= 0, as the reference's ``chi > 0``
+    test, or large enough) the contraction is exact and runs on the row-boundary
+    kernels (top/bottom boundary MPSs of bond D^(Lx/2-1), a column sweep through
+    the two middle rows, cached column environments); otherwise on the
+    chi-truncated kernels (vmc_peps_chi_*: each side's boundary as the full
+    vector over its D^Ly legs, truncated by Gram/Jacobi across the scheduled
+    cuts).  ``truncated`` tells which.
 
     precision="fp32": FP32 contraction with power-of-two rescaling per column
     (the production path); "fp64": FP64 (parity mode).
@@ -604,8 +608,14 @@ class FPEPS_GB300(WavefunctionModel_GB300):
                  generator=None, tensors=None, env_reuse=True, env_rows=2048):
         if precision not in _PEPS_PREC:
             raise ValueError("precision must be 'fp32' or 'fp64'")
-        if Lx % 2 or not 4 <= Lx <= 8 or D not in (2, 4) or D ** (Lx // 2 - 1) > 16 or Lx * Ly > 64:
-            raise ValueError("supported: even Lx in [4, 8], D in {2, 4}, D**(Lx/2-1) <= 16, Lx*Ly <= 64")
+        chi = int(max_bond) if max_bond is not None else 0
+        self.chi_cuts = self.chi_schedule(Lx, Ly, D, chi) if chi > 0 else []
+        self.truncated = any(self.chi_cuts)
+        if self.truncated:
+            if Lx % 2 or D not in (2, 4) or D ** Ly > 4096 or Lx * Ly > 64:
+                raise ValueError("chi-truncated fPEPS supports even Lx, D in {2, 4}, D**Ly <= 4096, Lx*Ly <= 64")
+        elif Lx % 2 or not 4 <= Lx <= 8 or D not in (2, 4) or D ** (Lx // 2 - 1) > 16 or Lx * Ly > 64:
+            raise ValueError("exact fPEPS supports even Lx in [4, 8], D in {2, 4}, D**(Lx/2-1) <= 16, Lx*Ly <= 64")
         if tensors is None:
             tensors = torch.randn((Lx, Ly, 4, D, D, D, D), generator=generator, dtype=torch.float64) * init_std
         tensors = torch.as_tensor(tensors, dtype=torch.float64).clone()
@@ -615,10 +625,35 @@ class FPEPS_GB300(WavefunctionModel_GB300):
         super().__init__([tensors.to(dtype)], Lx * Ly)
         self.Lx, self.Ly, self.D = Lx, Ly, D
         self.max_bond = max_bond
+        self.chi = chi
         self.precision = precision
         self.env_reuse = env_reuse
         self.env_rows = env_rows
+        self.chi_rows = 8192
         self._cast = None
+
+    @staticmethod
+    def chi_schedule(Lx, Ly, D, chi):
+        """Per absorbed row of a side, the cuts (columns to their left) that
+        the chi-truncated contraction truncates; empty lists everywhere mean
+        the contraction with max_bond = chi is exact."""
+        if Lx % 2 or D not in (2, 4) or D ** Ly > 4096 or Lx * Ly > 64 or chi < 1:
+            # outside the truncated kernels: exact only when no bond can exceed chi
+            return [[]] * (Lx // 2) if chi >= D ** (Lx // 2) else [[-1]]
+        cuts = (ctypes.c_uint32 * (Lx // 2))()
+        _lib.call("vmc_peps_chi_schedule", Lx, Ly, D, chi, cuts, Lx // 2)
+        return [[k for k in range(Ly - 1, 0, -1) if (cuts[a] >> k) & 1] for a in range(Lx // 2)]
+
+    def _chi_work(self, st, rows=None):
+        rows = int(rows or min(st.B, self.chi_rows))
+        nbytes = ctypes.c_int64(0)
+        _lib.call("vmc_peps_chi_work_bytes", self._prec, self.Lx, self.Ly, self.D, self.chi, rows,
+                  ctypes.byref(nbytes))
+        w = st.extra.get("chi_work")
+        if w is None or w.numel() < nbytes.value:
+            w = torch.empty(nbytes.value, dtype=torch.uint8, device=st.device)
+            st.extra["chi_work"] = w
+        return w, rows
 
     @staticmethod
     def structure_mask(Lx, Ly, D):
@@ -656,6 +691,11 @@ class FPEPS_GB300(WavefunctionModel_GB300):
 
     def _refresh(self, st, threshold):
         T = self._tensors(st.device)
+        if self.truncated:
+            work, rows = self._chi_work(st)
+            _lib.call("vmc_peps_chi_eval", self._prec, _lib.ptr(T), *self._shape_args(), self.chi, _lib.ptr(st.occ),
+                      st.B, _lib.ptr(st.sign), _lib.ptr(st.logabs), _lib.ptr(work), rows, _lib.stream_of(st.device))
+            return
         _lib.call("vmc_peps_eval", self._prec, _lib.ptr(T), *self._shape_args(), _lib.ptr(st.occ), st.B,
                   _lib.ptr(st.sign), _lib.ptr(st.logabs), _lib.stream_of(st.device))
 
@@ -674,6 +714,14 @@ class FPEPS_GB300(WavefunctionModel_GB300):
             for a in (rm, rb, ra):
                 if tuple(a.shape) != (n_sweeps, E, st.B) or not a.is_cuda or not a.is_contiguous():
                     raise ValueError("replay buffers must be contiguous CUDA tensors of shape (n_sweeps, E, B)")
+        if self.truncated:
+            work, rows = self._chi_work(st)
+            _lib.call("vmc_peps_chi_sweep", self._prec, _lib.ptr(T), *self._shape_args(), self.chi, _lib.ptr(st.occ),
+                      st.B, _lib.ptr(edges), edges.shape[0], int(n_sweeps), float(hopping_rate),
+                      int(seed) & ((1 << 64) - 1), int(sweep_offset), _lib.ptr(rm), _lib.ptr(rb), _lib.ptr(ra),
+                      _lib.ptr(st.sign), _lib.ptr(st.logabs), _lib.ptr(st.n_acc), _lib.ptr(n_eval), _lib.ptr(work),
+                      rows, _lib.stream_of(st.device))
+            return
         work, rows, err = self._env_work(st)
         _lib.call("vmc_peps_sweep", self._prec, _lib.ptr(T), *self._shape_args(), _lib.ptr(st.occ), st.B,
                   _lib.ptr(edges), edges.shape[0], int(n_sweeps), float(hopping_rate), int(seed) & ((1 << 64) - 1),
@@ -711,6 +759,14 @@ class FPEPS_GB300(WavefunctionModel_GB300):
         pairs, offs, P = self.conn_pairs(st, H)
         term = torch.empty(max(P, 1), dtype=torch.float64, device=st.device)
         eloc = torch.empty(st.B, dtype=torch.float64, device=st.device)
+        if self.truncated:
+            work, rows = self._chi_work(st)
+            offs_h = offs.cpu()
+            _lib.call("vmc_peps_chi_local_energy", self._prec, _lib.ptr(T), *self._shape_args(), self.chi,
+                      _lib.ptr(st.occ), st.B, _lib.ptr(edges), float(H.t), float(H.U), _lib.ptr(pairs), _lib.ptr(offs),
+                      ctypes.c_void_p(offs_h.data_ptr()), P, _lib.ptr(term), _lib.ptr(eloc), _lib.ptr(work), rows,
+                      _lib.stream_of(st.device))
+            return eloc
         work, rows, err = self._env_work(st)
         _lib.call("vmc_peps_local_energy", self._prec, _lib.ptr(T), *self._shape_args(), _lib.ptr(st.occ), st.B,
                   _lib.ptr(edges), float(H.t), float(H.U), _lib.ptr(st.sign), _lib.ptr(st.logabs), _lib.ptr(pairs),
@@ -723,6 +779,9 @@ class FPEPS_GB300(WavefunctionModel_GB300):
         """O (B, n_params) = d log|psi| / d tensors (flattened parameter order),
         FP32 for precision "fp32", FP64 for "fp64"; hand-written reverse
         column sweep (vmc_peps_logpsi_grad)."""
+        if self.truncated:
+            raise NotImplementedError("log-derivatives through the chi-truncated boundary contraction are not "
+                                      "implemented; use max_bond >= D**(Lx//2) (exact contraction) for SR")
         T = self._tensors(st.device)
         dt = torch.float32 if self._prec == 0 else torch.float64
         if out is None:
