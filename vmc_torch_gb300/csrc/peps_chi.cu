@@ -68,10 +68,8 @@ __device__ __forceinline__ uint32_t block_member(int b, int i) {
 
 template <typename T>
 struct ChiSmem {
-  // W: D * NS, A: D^4, S and V: 2 x 32 x 33 each, lam: 64, keep: 64 ints, red: 32
-  static size_t bytes(int NS, int D) {
-    return ((size_t)D * NS + (size_t)D * D * D * D + 4 * 32 * 33 + 64 + 32) * sizeof(T) + 64 * sizeof(int) + 16;
-  }
+  // absorption: W (D * NS), the two parity blocks of A ((D^2/2)^2 each), reduction scratch
+  static size_t bytes(int NS, int D) { return ((size_t)D * NS + (size_t)D * D * D * D / 2 + 32) * sizeof(T) + 16; }
 };
 
 // One warp: eigen-decomposition of the symmetric 32 x 32 matrix in S (row
@@ -165,157 +163,117 @@ __device__ T cta_absmax(T m, T* red) {
   return r;
 }
 
-// Truncate the state psi = W[0 .. NS) to rank chi across the cut after k columns.
-template <typename T, int D>
-__device__ void chi_truncate(T* W, int NS, int Ly, int k, int chi, T* S, T* V, T* lam, int* keep) {
-  int nL = 1;
-  for (int i = 0; i < k; ++i) nL *= D;
-  const int nR = NS / nL;
-  const bool left = nL <= nR;
-  const int n = left ? nL : nR, nb = n >> 1, big = NS / n;
-  auto at = [&](uint32_t p, int q) -> int { return left ? (int)p * nR + q : q * nR + (int)p; };
-  T* Y = W + NS;  // the h = 1 slice is free between rows
-  // Gram blocks, zero-padded to 32 x 32
-  for (int e = threadIdx.x; e < 2 * 32 * 33; e += blockDim.x) S[e] = T(0);
-  __syncthreads();
-  const int tri = nb * (nb + 1) / 2;
-  for (int e = threadIdx.x; e < 2 * tri; e += blockDim.x) {
-    const int b = e / tri;
-    int r = e - b * tri, i = 0;
-    while (r > i) { r -= i + 1; ++i; }
-    const int j = r;
-    const uint32_t pi = block_member<D>(b, i), pj = block_member<D>(b, j);
-    T acc = T(0);
-    for (int q = 0; q < big; ++q) acc += W[at(pi, q)] * W[at(pj, q)];
-    S[b * 32 * 33 + i * 33 + j] = acc;
-    S[b * 32 * 33 + j * 33 + i] = acc;
-  }
-  __syncthreads();
-  const int warp = threadIdx.x >> 5;
-  if (warp < 2) warp_jacobi<T>(S + warp * 32 * 33, V + warp * 32 * 33, lam + warp * 32);
-  __syncthreads();
-  if (threadIdx.x < 64) {
-    const int b = threadIdx.x >> 5, i = threadIdx.x & 31;
-    int kp = 0;
-    if (i < nb) {
-      const T l = lam[b * 32 + i];
-      int rank = 0;
-      for (int e = 0; e < 64; ++e) {
-        const int b2 = e >> 5, i2 = e & 31;
-        if (i2 >= nb) continue;
-        const T l2 = lam[e];
-        rank += (l2 > l) || (l2 == l && (b2 < b || (b2 == b && i2 < i)));
-      }
-      kp = rank < chi;
-    }
-    keep[threadIdx.x] = kp;
-  }
-  __syncthreads();
-  // Y[b][i][q] = v_i . psi_b(:, q) for kept i
-  for (int e = threadIdx.x; e < NS; e += blockDim.x) {
-    const int bi = e / big, q = e - bi * big, b = bi / nb, i = bi - b * nb;
-    T acc = T(0);
-    if (keep[b * 32 + i]) {
-      const T* vi = V + b * 32 * 33 + i * 33;
-      for (int j = 0; j < nb; ++j) acc += vi[j] * W[at(block_member<D>(b, j), q)];
-    }
-    Y[e] = acc;
-  }
-  __syncthreads();
-  // psi_b(p_j, q) = sum_i v_i[j] Y[b][i][q]
-  for (int e = threadIdx.x; e < NS; e += blockDim.x) {
-    const int bj = e / big, q = e - bj * big, b = bj / nb, j = bj - b * nb;
-    T acc = T(0);
-    for (int i = 0; i < nb; ++i)
-      if (keep[b * 32 + i]) acc += V[b * 32 * 33 + i * 33 + j] * Y[(b * nb + i) * big + q];
-    W[at(block_member<D>(b, j), q)] = acc;
-  }
-  __syncthreads();
-  for (int e = threadIdx.x; e < NS; e += blockDim.x) Y[e] = T(0);
-  __syncthreads();
+// Item -> (configuration index ci, side): sides == nullptr: ci = item >> 1,
+// side = item & 1; else ci = cfg_idx[item] (or item), side = sides[item].  The
+// item's state lives in slot 2 * ci + side.
+__device__ __forceinline__ void chi_item(int64_t item, const int32_t* cfg_idx, const uint8_t* sides, int64_t& ci,
+                                         int& side) {
+  if (sides) { ci = cfg_idx ? cfg_idx[item] : item; side = sides[item]; }
+  else { ci = item >> 1; side = (int)(item & 1); }
 }
 
-// Boundary state of one side for one configuration.  item -> configuration
-// cfg[2 * ci], side (0 = top rows [0, Lx/2), 1 = bottom rows [Lx/2, Lx)):
-// sides == nullptr: ci = item >> 1, side = item & 1; else ci = cfg_idx[item]
-// (or item when cfg_idx is null), side = sides[item].  The state goes to slot
-// 2 * ci + side of out / expo_out.  count: optional device item count (items
-// past it exit).
+// Electron parity of the first n_rows rows of a side.
+__device__ __forceinline__ int side_parity(uint64_t up, uint64_t dn, int Lx, int Ly, int side, int n_rows) {
+  const int r0 = side ? Lx - n_rows : 0;
+  const uint64_t m = bits_below((r0 + n_rows) * Ly) & ~bits_below(r0 * Ly);
+  return (__popcll(up & m) + __popcll(dn & m)) & 1;
+}
+
+// Absorbs rows [a0, a1) of each item's side into its boundary state (slot
+// 2 ci + side of state / expo; a0 == 0 starts from the empty boundary).  One
+// CTA per item, W[h][idx] (D x NS) in shared memory.  Z2 structure: while a
+// row is absorbed, W[h][idx] vanishes unless p(h) + p(idx) equals the parity
+// of the electrons absorbed so far, and A[h][o][h'][n] unless p(h) + p(o) +
+// p(h') + p(n) equals the site's; so a group's D^2 inputs hold D^2/2 non-zero
+// values, mapped by a (D^2/2)^2 block of A onto the D^2/2 outputs of the
+// other class when the site's parity is odd (the emptied slots are zeroed).
 template <typename T, int D>
 __global__ void __launch_bounds__(CHI_NT)
-    k_chi_side(const T* __restrict__ tens, ChiSched sc, const uint64_t* __restrict__ cfg,
-               const int32_t* __restrict__ cfg_idx, const uint8_t* __restrict__ sides, int64_t n_items,
-               const int* __restrict__ count, T* __restrict__ out, int* __restrict__ expo_out) {
+    k_chi_absorb(const T* __restrict__ tens, ChiSched sc, const uint64_t* __restrict__ cfg,
+                 const int32_t* __restrict__ cfg_idx, const uint8_t* __restrict__ sides, int64_t n_items,
+                 const int* __restrict__ count, int a0, int a1, T* __restrict__ state, int* __restrict__ expo_io) {
+  constexpr int H = D * D / 2;  // non-zero entries of a group
   extern __shared__ __align__(16) unsigned char smraw[];
   const int64_t item = blockIdx.x;
   if (item >= n_items || (count && item >= *count)) return;
   const int NS = sc.NS, Ly = sc.Ly, Lx = sc.Lx;
   T* W = reinterpret_cast<T*>(smraw);
-  T* A = W + (size_t)D * NS;
-  T* S = A + D * D * D * D;
-  T* V = S + 2 * 32 * 33;
-  T* lam = V + 2 * 32 * 33;
-  T* red = lam + 64;
-  int* keep = reinterpret_cast<int*>(red + 32);
+  T* A2 = W + (size_t)D * NS;   // [class of (o, h)][H][H]
+  T* red = A2 + 2 * H * H;
   int64_t ci;
   int side;
-  if (sides) { ci = cfg_idx ? cfg_idx[item] : item; side = sides[item]; }
-  else { ci = item >> 1; side = (int)(item & 1); }
+  chi_item(item, cfg_idx, sides, ci, side);
+  const int64_t slot = 2 * ci + side;
   const uint64_t up = cfg[2 * ci], dn = cfg[2 * ci + 1];
-  for (int e = threadIdx.x; e < D * NS; e += blockDim.x) W[e] = (e == 0) ? T(1) : T(0);
+  T* st = state + slot * (int64_t)NS;
   int expo = 0;
   bool zero = false, bad = false;
-  for (int a = 0; a < sc.rows && !zero && !bad; ++a) {
+  if (a0 == 0) {
+    for (int e = threadIdx.x; e < D * NS; e += blockDim.x) W[e] = (e == 0) ? T(1) : T(0);
+  } else {
+    expo = expo_io[slot];
+    zero = expo == CHI_EXP_ZERO;
+    bad = expo == CHI_EXP_BAD;
+    for (int e = threadIdx.x; e < D * NS; e += blockDim.x) W[e] = (e < NS && !zero && !bad) ? st[e] : T(0);
+  }
+  int par = side_parity(up, dn, Lx, Ly, side, a0);
+  for (int a = a0; a < a1 && !zero && !bad; ++a) {
     const int r = side ? (Lx - 1 - a) : a;
     int nleft = 0;
     int stride = NS / D;
     for (int c = 0; c < Ly; ++c, stride /= D) {
       const int site = r * Ly + c;
       const int x = site_state(up, dn, site);
+      const int px = (x ^ (x >> 1)) & 1;
       __syncthreads();
       const T* ts = tens + ((size_t)site * 4 + x) * (D * D * D * D);
-      for (int e = threadIdx.x; e < D * D * D * D; e += blockDim.x) {
-        const int n = e % D, hp = (e / D) % D, o = (e / (D * D)) % D, h = e / (D * D * D);
+      for (int e = threadIdx.x; e < 2 * H * H; e += blockDim.x) {
+        // input pair ia = (o, h) of class ti, output pair ib = (n, h') of class ti ^ px
+        const int ti = e / (H * H), ia = (e / H) % H, ib = e % H;
+        const int o = ia / (D / 2), h = ((ti ^ (o & 1)) & 1) + 2 * (ia % (D / 2));
+        const int to = ti ^ px;
+        const int n = ib / (D / 2), hp = ((to ^ (n & 1)) & 1) + 2 * (ib % (D / 2));
         const int u = side ? n : o, d = side ? o : n;
         T val = ts[((h * D + u) * D + hp) * D + d];
         if (r >= 1 && (u & 1) && ((h + nleft) & 1)) val = -val;
-        A[e] = val;
+        A2[e] = val;
       }
       __syncthreads();
       for (int gi = threadIdx.x; gi < NS / D; gi += blockDim.x) {
         const int lo = gi % stride, hi = gi / stride;
         const int base = hi * stride * D + lo;
-        T in[D][D];
+        const int ti = (par ^ digit_parity<D>((uint32_t)base)) & 1, to = ti ^ px;
+        T in[H];
         bool any = false;
 #pragma unroll
-        for (int o = 0; o < D; ++o)
-#pragma unroll
-          for (int hh = 0; hh < D; ++hh) {
-            in[o][hh] = W[hh * NS + base + o * stride];
-            any |= in[o][hh] != T(0);
-          }
+        for (int ia = 0; ia < H; ++ia) {
+          const int o = ia / (D / 2), h = ((ti ^ (o & 1)) & 1) + 2 * (ia % (D / 2));
+          in[ia] = W[h * NS + base + o * stride];
+          any |= in[ia] != T(0);
+        }
         if (!any) continue;
-        T outv[D][D];
+        const T* Ab = A2 + ti * H * H;
+        T outv[H];
 #pragma unroll
-        for (int nn = 0; nn < D; ++nn)
+        for (int ib = 0; ib < H; ++ib) outv[ib] = T(0);
 #pragma unroll
-          for (int hp = 0; hp < D; ++hp) outv[nn][hp] = T(0);
+        for (int ia = 0; ia < H; ++ia)
 #pragma unroll
-        for (int hh = 0; hh < D; ++hh)
+          for (int ib = 0; ib < H; ++ib) outv[ib] += in[ia] * Ab[ia * H + ib];
+        if (px) {  // the input class empties
 #pragma unroll
-          for (int o = 0; o < D; ++o) {
-            const T a0 = in[o][hh];
-            const T* Ar = A + (hh * D + o) * D * D;
-#pragma unroll
-            for (int hp = 0; hp < D; ++hp)
-#pragma unroll
-              for (int nn = 0; nn < D; ++nn) outv[nn][hp] += a0 * Ar[hp * D + nn];
+          for (int ia = 0; ia < H; ++ia) {
+            const int o = ia / (D / 2), h = ((ti ^ (o & 1)) & 1) + 2 * (ia % (D / 2));
+            W[h * NS + base + o * stride] = T(0);
           }
+        }
 #pragma unroll
-        for (int nn = 0; nn < D; ++nn)
-#pragma unroll
-          for (int hp = 0; hp < D; ++hp) W[hp * NS + base + nn * stride] = outv[nn][hp];
+        for (int ib = 0; ib < H; ++ib) {
+          const int n = ib / (D / 2), hp = ((to ^ (n & 1)) & 1) + 2 * (ib % (D / 2));
+          W[hp * NS + base + n * stride] = outv[ib];
+        }
       }
+      par ^= px;
       nleft += __popcll((up >> site) & 1ull) + __popcll((dn >> site) & 1ull);
     }
     __syncthreads();
@@ -323,9 +281,9 @@ __global__ void __launch_bounds__(CHI_NT)
     T m = T(0);
     int nonfinite = 0;
     for (int e = threadIdx.x; e < NS; e += blockDim.x) {
-      const T x = fabs(W[e]);
-      nonfinite |= !(x < T(INFINITY));
-      m = fmax(m, x);
+      const T v = fabs(W[e]);
+      nonfinite |= !(v < T(INFINITY));
+      m = fmax(m, v);
     }
     if (__syncthreads_or(nonfinite)) { bad = true; break; }
     m = cta_absmax<T>(m, red);
@@ -334,15 +292,113 @@ __global__ void __launch_bounds__(CHI_NT)
     expo += e2;
     __syncthreads();
     for (int e = threadIdx.x; e < NS; e += blockDim.x) W[e] = scalbn(W[e], -e2);
-    __syncthreads();
-    for (int k = Ly - 1; k >= 1; --k)
-      if ((sc.cuts[a] >> k) & 1u) chi_truncate<T, D>(W, NS, Ly, k, sc.chi, S, V, lam, keep);
   }
   __syncthreads();
-  const int64_t slot = sides ? 2 * ci + side : item;
-  T* dst = out + slot * (int64_t)NS;
-  for (int e = threadIdx.x; e < NS; e += blockDim.x) dst[e] = (zero || bad) ? T(0) : W[e];
-  if (threadIdx.x == 0) expo_out[slot] = bad ? CHI_EXP_BAD : (zero ? CHI_EXP_ZERO : expo);
+  for (int e = threadIdx.x; e < NS; e += blockDim.x) st[e] = (zero || bad) ? T(0) : W[e];
+  if (threadIdx.x == 0) expo_io[slot] = bad ? CHI_EXP_BAD : (zero ? CHI_EXP_ZERO : expo);
+}
+
+constexpr int CHI_TRUNC_ITEMS = 4;  // items per CTA, two warps (one per parity block) each
+
+template <typename T>
+struct ChiTruncSmem {
+  static size_t bytes() { return (size_t)CHI_TRUNC_ITEMS * ((4 * 32 * 33 + 64) * sizeof(T) + 64 * sizeof(int)); }
+};
+
+// Best rank-chi truncation across cut k of each item's state (after the
+// side's first n_rows rows): warp b of an item forms the parity block b of the
+// Gram matrix on the cut's smaller side (only the big-side indices of the
+// matching parity contribute), diagonalises it (warp_jacobi), and after the
+// item's two warps have ranked their eigenvalues together projects its block
+// of the state onto the kept eigenvectors.  The state stays in global memory
+// (L2-resident).
+template <typename T, int D>
+__global__ void __launch_bounds__(32 * 2 * CHI_TRUNC_ITEMS)
+    k_chi_trunc(ChiSched sc, int k, int n_rows, const uint64_t* __restrict__ cfg,
+                const int32_t* __restrict__ cfg_idx, const uint8_t* __restrict__ sides, int64_t n_items,
+                const int* __restrict__ count, T* __restrict__ state, const int* __restrict__ expo_io) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int warp = threadIdx.x >> 5, ln = threadIdx.x & 31;
+  const int il = warp >> 1, b = warp & 1;
+  const int64_t item = (int64_t)blockIdx.x * CHI_TRUNC_ITEMS + il;
+  const int64_t lim = count ? (int64_t)*count : n_items;
+  const bool live = item < n_items && item < lim;
+  T* base_s = reinterpret_cast<T*>(smraw) + (size_t)il * (4 * 32 * 33 + 64);
+  T* S = base_s + b * 32 * 33;
+  T* V = base_s + 2 * 32 * 33 + b * 32 * 33;
+  T* lam = base_s + 4 * 32 * 33;  // [2][32]
+  int* keep = reinterpret_cast<int*>(reinterpret_cast<T*>(smraw) + (size_t)CHI_TRUNC_ITEMS * (4 * 32 * 33 + 64)) +
+              il * 64;
+  const int NS = sc.NS;
+  int nL = 1;
+  for (int i = 0; i < k; ++i) nL *= D;
+  const int nR = NS / nL;
+  const bool left = nL <= nR;
+  const int n = left ? nL : nR, nb = n >> 1, nq = (NS / n) >> 1;
+  int64_t ci = 0;
+  int side = 0, qcls = 0;
+  bool on = false;
+  T* st = nullptr;
+  if (live) {
+    chi_item(item, cfg_idx, sides, ci, side);
+    const int ex = expo_io[2 * ci + side];
+    on = ex != CHI_EXP_ZERO && ex != CHI_EXP_BAD;
+    st = state + (2 * ci + side) * (int64_t)NS;
+    qcls = side_parity(cfg[2 * ci], cfg[2 * ci + 1], sc.Lx, sc.Ly, side, n_rows) ^ b;
+  }
+  const uint32_t pi = block_member<D>(b, ln);
+  auto at = [&](uint32_t p, uint32_t q) -> int64_t {
+    return left ? (int64_t)p * nR + q : (int64_t)q * nR + p;
+  };
+  // Gram block: lane i accumulates row i
+  {
+    T acc[32];
+#pragma unroll
+    for (int j = 0; j < 32; ++j) acc[j] = T(0);
+    if (on)
+      for (int iq = 0; iq < nq; ++iq) {
+        const uint32_t q = block_member<D>(qcls, iq);
+        const T a = (ln < nb) ? st[at(pi, q)] : T(0);
+#pragma unroll
+        for (int j = 0; j < 32; ++j) acc[j] += a * __shfl_sync(VMC_FULL_MASK, a, j);
+      }
+#pragma unroll
+    for (int j = 0; j < 32; ++j) S[ln * 33 + j] = acc[j];
+  }
+  __syncwarp();
+  warp_jacobi<T>(S, V, lam + b * 32);
+  __syncthreads();
+  {
+    const T l = lam[b * 32 + ln];
+    int rank = 0;
+    for (int e = 0; e < 64; ++e) {
+      const int b2 = e >> 5, i2 = e & 31;
+      if (i2 >= nb) continue;
+      const T l2 = lam[e];
+      rank += (l2 > l) || (l2 == l && (b2 < b || (b2 == b && i2 < ln)));
+    }
+    keep[b * 32 + ln] = (ln < nb) && rank < sc.chi;
+  }
+  __syncwarp();
+  // projection of the block onto the kept eigenvectors, one big-side column at a time
+  if (on) {
+    T vi[32];
+#pragma unroll
+    for (int j = 0; j < 32; ++j) vi[j] = V[ln * 33 + j];
+    const bool kp = keep[b * 32 + ln] != 0;
+    for (int iq = 0; iq < nq; ++iq) {
+      const uint32_t q = block_member<D>(qcls, iq);
+      const T a = (ln < nb) ? st[at(pi, q)] : T(0);
+      T y = T(0);
+#pragma unroll
+      for (int j = 0; j < 32; ++j) y += vi[j] * __shfl_sync(VMC_FULL_MASK, a, j);
+      if (!kp) y = T(0);
+      T nv = T(0);
+#pragma unroll
+      for (int i = 0; i < 32; ++i) nv += V[i * 33 + ln] * __shfl_sync(VMC_FULL_MASK, y, i);
+      if (ln < nb) st[at(pi, q)] = nv;
+    }
+  }
 }
 
 // (sign, log|psi|) from <top, bottom> * 2^(et + eb) and the global sign.
@@ -613,24 +669,42 @@ int chi_plan(int Lx, int Ly, int D, int chi, ChiSched& sc) {
   return VMC_OK;
 }
 
+template <typename T, int D>
+int build_sides_d(const void* tens, const ChiSched& sc, const uint64_t* cfg, const int32_t* cfg_idx,
+                  const uint8_t* sides, int64_t n_items, const int* count, T* state, int* ex, cudaStream_t st) {
+  const size_t smem = ChiSmem<T>::bytes(sc.NS, D);
+  if (cudaFuncSetAttribute(k_chi_absorb<T, D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return VMC_ERR_CUDA;
+  const size_t tsm = ChiTruncSmem<T>::bytes();
+  if (cudaFuncSetAttribute(k_chi_trunc<T, D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm) != cudaSuccess)
+    return VMC_ERR_CUDA;
+  int a = 0;
+  while (a < sc.rows) {
+    int a1 = a + 1;
+    while (a1 < sc.rows && sc.cuts[a1 - 1] == 0) ++a1;
+    k_chi_absorb<T, D><<<(unsigned)n_items, CHI_NT, smem, st>>>((const T*)tens, sc, cfg, cfg_idx, sides, n_items,
+                                                                count, a, a1, state, ex);
+    VMC_CUDA_CHECK_LAUNCH();
+    for (int k = sc.Ly - 1; k >= 1; --k)
+      if ((sc.cuts[a1 - 1] >> k) & 1u) {
+        k_chi_trunc<T, D><<<(unsigned)((n_items + CHI_TRUNC_ITEMS - 1) / CHI_TRUNC_ITEMS), 64 * CHI_TRUNC_ITEMS, tsm,
+                            st>>>(sc, k, a1, cfg, cfg_idx, sides, n_items, count, state, ex);
+        VMC_CUDA_CHECK_LAUNCH();
+      }
+    a = a1;
+  }
+  return VMC_OK;
+}
+
+// Boundary states of n_items (configuration, side) items into slots
+// 2 ci + side of state / ex: the rows of the schedule absorbed in runs that
+// end at a row with truncated cuts, each cut then truncated.
 template <typename T>
 int launch_chi_side(const void* tens, const ChiSched& sc, const uint64_t* cfg, const int32_t* cfg_idx,
-                    const uint8_t* sides, int64_t n_items, const int* count, T* out, int* ex, cudaStream_t st) {
+                    const uint8_t* sides, int64_t n_items, const int* count, T* state, int* ex, cudaStream_t st) {
   if (n_items <= 0) return VMC_OK;
-  const size_t smem = ChiSmem<T>::bytes(sc.NS, sc.D);
-  if (sc.D == 4) {
-    if (cudaFuncSetAttribute(k_chi_side<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-      return VMC_ERR_CUDA;
-    k_chi_side<T, 4><<<(unsigned)n_items, CHI_NT, smem, st>>>((const T*)tens, sc, cfg, cfg_idx, sides, n_items,
-                                                               count, out, ex);
-  } else {
-    if (cudaFuncSetAttribute(k_chi_side<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-      return VMC_ERR_CUDA;
-    k_chi_side<T, 2><<<(unsigned)n_items, CHI_NT, smem, st>>>((const T*)tens, sc, cfg, cfg_idx, sides, n_items,
-                                                               count, out, ex);
-  }
-  VMC_CUDA_CHECK_LAUNCH();
-  return VMC_OK;
+  return sc.D == 4 ? build_sides_d<T, 4>(tens, sc, cfg, cfg_idx, sides, n_items, count, state, ex, st)
+                   : build_sides_d<T, 2>(tens, sc, cfg, cfg_idx, sides, n_items, count, state, ex, st);
 }
 
 
