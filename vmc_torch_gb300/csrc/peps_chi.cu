@@ -113,11 +113,12 @@ __device__ void warp_jacobi(T* S, T* V, T* lam) {
       if (!lead) { c = c2; s = s2; need = n2; }
       if (!__any_sync(VMC_FULL_MASK, need)) continue;
       rotated = true;
+      const T sp = lead ? -s : s;  // row p' = c p - s q, row q' = s p + c q
       // rows: H = J^T G
 #pragma unroll
       for (int j = 0; j < 32; ++j) {
         const T o = __shfl_xor_sync(VMC_FULL_MASK, g[j], m);
-        g[j] = lead ? (c * g[j] - s * o) : (s * o + c * g[j]);
+        g[j] = fma(sp, o, c * g[j]);
       }
       __syncwarp();
 #pragma unroll
@@ -130,7 +131,7 @@ __device__ void warp_jacobi(T* S, T* V, T* lam) {
 #pragma unroll
       for (int j = 0; j < 32; ++j) {
         const T o = __shfl_xor_sync(VMC_FULL_MASK, g[j], m);
-        g[j] = lead ? (c * g[j] - s * o) : (s * o + c * g[j]);
+        g[j] = fma(sp, o, c * g[j]);
       }
 #pragma unroll
       for (int j = 0; j < 32; ++j) S[ln * 33 + j] = g[j];
@@ -139,7 +140,7 @@ __device__ void warp_jacobi(T* S, T* V, T* lam) {
 #pragma unroll
       for (int j = 0; j < 32; ++j) {
         const T o = __shfl_xor_sync(VMC_FULL_MASK, v[j], m);
-        v[j] = lead ? (c * v[j] - s * o) : (s * o + c * v[j]);
+        v[j] = fma(sp, o, c * v[j]);
       }
     }
     if (!rotated) break;
@@ -147,6 +148,74 @@ __device__ void warp_jacobi(T* S, T* V, T* lam) {
   lam[ln] = S[ln * 33 + ln];
 #pragma unroll
   for (int j = 0; j < 32; ++j) V[ln * 33 + j] = v[j];
+  __syncwarp();
+}
+
+// One warp: one-sided (Hestenes) Jacobi on the rows u_i (lane i, up to 32
+// columns) of a block of the state.  Pairs (i, i xor m) are rotated until
+// their rows are orthogonal; the accumulated rotation Q (lane i holds row i)
+// satisfies Q A = U with orthogonal rows, so the rows of Q are the
+// eigenvectors of A A^T with eigenvalues |u_i|^2.  Works on A itself, so the
+// condition number is not squared as in the Gram matrix.  Output as
+// warp_jacobi: lam[i], V[i * 33 + j] = Q[i][j].
+template <typename T>
+__device__ void warp_hestenes(T (&u)[32], T* V, T* lam) {
+  const int ln = threadIdx.x & 31;
+  T qv[32];
+#pragma unroll
+  for (int j = 0; j < 32; ++j) qv[j] = (j == ln) ? T(1) : T(0);
+  const T tol = std::is_same<T, float>::value ? T(2e-7) : T(4e-16);
+  T nrm = T(0);
+#pragma unroll
+  for (int j = 0; j < 32; ++j) nrm = fma(u[j], u[j], nrm);
+  T floor_ = nrm;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) floor_ = fmax(floor_, __shfl_xor_sync(VMC_FULL_MASK, floor_, o));
+  floor_ *= tol;
+  for (int sw = 0; sw < 20; ++sw) {
+    bool rotated = false;
+    for (int m = 1; m < 32; ++m) {
+      const bool lead = ln < (ln ^ m);
+      T o[32];
+      T gam = T(0), alp = T(0);
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {
+        o[j] = __shfl_xor_sync(VMC_FULL_MASK, u[j], m);
+        gam = fma(u[j], o[j], gam);
+        alp = fma(u[j], u[j], alp);
+      }
+      const T bet = __shfl_xor_sync(VMC_FULL_MASK, alp, m);
+      T c = T(1), s = T(0);
+      int need = 0;
+      if (lead && fabs(gam) > floor_ && fabs(gam) > tol * sqrt(alp * bet)) {
+        const T zeta = (bet - alp) / (T(2) * gam);
+        const T t = (zeta >= T(0) ? T(1) : T(-1)) / (fabs(zeta) + hypot(T(1), zeta));
+        c = T(1) / sqrt(T(1) + t * t);
+        s = t * c;
+        need = 1;
+      }
+      const T c2 = __shfl_xor_sync(VMC_FULL_MASK, c, m), s2 = __shfl_xor_sync(VMC_FULL_MASK, s, m);
+      const int n2 = __shfl_xor_sync(VMC_FULL_MASK, need, m);
+      if (!lead) { c = c2; s = s2; need = n2; }
+      if (!__any_sync(VMC_FULL_MASK, need)) continue;
+      rotated = true;
+      const T sp = lead ? -s : s;
+#pragma unroll
+      for (int j = 0; j < 32; ++j) u[j] = fma(sp, o[j], c * u[j]);
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {
+        const T oq = __shfl_xor_sync(VMC_FULL_MASK, qv[j], m);
+        qv[j] = fma(sp, oq, c * qv[j]);
+      }
+    }
+    if (!rotated) break;
+  }
+  nrm = T(0);
+#pragma unroll
+  for (int j = 0; j < 32; ++j) nrm = fma(u[j], u[j], nrm);
+  lam[ln] = nrm;
+#pragma unroll
+  for (int j = 0; j < 32; ++j) V[ln * 33 + j] = qv[j];
   __syncwarp();
 }
 
@@ -350,8 +419,15 @@ __global__ void __launch_bounds__(32 * 2 * CHI_TRUNC_ITEMS)
   auto at = [&](uint32_t p, uint32_t q) -> int64_t {
     return left ? (int64_t)p * nR + q : (int64_t)q * nR + p;
   };
-  // Gram block: lane i accumulates row i
-  {
+  if (nq <= 32) {
+    // the block fits a warp's registers (the middle cut of a 6-wide lattice): one-sided Jacobi on its rows
+    T u[32];
+#pragma unroll
+    for (int j = 0; j < 32; ++j)
+      u[j] = (on && ln < nb && j < nq) ? st[at(pi, block_member<D>(qcls, j))] : T(0);
+    warp_hestenes<T>(u, V, lam + b * 32);
+  } else {
+    // Gram block: lane i accumulates row i
     T acc[32];
 #pragma unroll
     for (int j = 0; j < 32; ++j) acc[j] = T(0);
@@ -364,9 +440,9 @@ __global__ void __launch_bounds__(32 * 2 * CHI_TRUNC_ITEMS)
       }
 #pragma unroll
     for (int j = 0; j < 32; ++j) S[ln * 33 + j] = acc[j];
+    __syncwarp();
+    warp_jacobi<T>(S, V, lam + b * 32);
   }
-  __syncwarp();
-  warp_jacobi<T>(S, V, lam + b * 32);
   __syncthreads();
   {
     const T l = lam[b * 32 + ln];
