@@ -68,8 +68,10 @@ __device__ __forceinline__ uint32_t block_member(int b, int i) {
 
 template <typename T>
 struct ChiSmem {
-  // absorption: W (D * NS), the two parity blocks of A ((D^2/2)^2 each), reduction scratch
-  static size_t bytes(int NS, int D) { return ((size_t)D * NS + (size_t)D * D * D * D / 2 + 32) * sizeof(T) + 16; }
+  // absorption: W (D * NS), per column of a row the two parity blocks of A ((D^2/2)^2 each), reduction scratch
+  static size_t bytes(int NS, int D, int Ly) {
+    return ((size_t)D * NS + (size_t)Ly * D * D * D * D / 2 + 32) * sizeof(T) + 16;
+  }
 };
 
 // One warp: eigen-decomposition of the symmetric 32 x 32 matrix in S (row
@@ -267,8 +269,8 @@ __global__ void __launch_bounds__(CHI_NT)
   if (item >= n_items || (count && item >= *count)) return;
   const int NS = sc.NS, Ly = sc.Ly, Lx = sc.Lx;
   T* W = reinterpret_cast<T*>(smraw);
-  T* A2 = W + (size_t)D * NS;   // [class of (o, h)][H][H]
-  T* red = A2 + 2 * H * H;
+  T* A2 = W + (size_t)D * NS;   // per column of the row: [class of (o, h)][H][H]
+  T* red = A2 + (size_t)sc.Ly * 2 * H * H;
   int64_t ci;
   int side;
   chi_item(item, cfg_idx, sides, ci, side);
@@ -288,25 +290,30 @@ __global__ void __launch_bounds__(CHI_NT)
   int par = side_parity(up, dn, Lx, Ly, side, a0);
   for (int a = a0; a < a1 && !zero && !bad; ++a) {
     const int r = side ? (Lx - 1 - a) : a;
-    int nleft = 0;
+    // the row's signed tensors, all columns at once (one global-load latency per row)
+    __syncthreads();
+    for (int e = threadIdx.x; e < Ly * 2 * H * H; e += blockDim.x) {
+      const int c = e / (2 * H * H), el = e - c * 2 * H * H;
+      const int site = r * Ly + c;
+      const int x = site_state(up, dn, site);
+      const int px = (x ^ (x >> 1)) & 1;
+      const uint64_t lm = bits_below(site) & ~bits_below(r * Ly);
+      const int nleft = __popcll(up & lm) + __popcll(dn & lm);
+      // input pair ia = (o, h) of class ti, output pair ib = (n, h') of class ti ^ px
+      const int ti = el / (H * H), ia = (el / H) % H, ib = el % H;
+      const int o = ia / (D / 2), h = ((ti ^ (o & 1)) & 1) + 2 * (ia % (D / 2));
+      const int to = ti ^ px;
+      const int n = ib / (D / 2), hp = ((to ^ (n & 1)) & 1) + 2 * (ib % (D / 2));
+      const int u = side ? n : o, d = side ? o : n;
+      T val = tens[((size_t)site * 4 + x) * (D * D * D * D) + ((h * D + u) * D + hp) * D + d];
+      if (r >= 1 && (u & 1) && ((h + nleft) & 1)) val = -val;
+      A2[e] = val;
+    }
     int stride = NS / D;
     for (int c = 0; c < Ly; ++c, stride /= D) {
       const int site = r * Ly + c;
       const int x = site_state(up, dn, site);
       const int px = (x ^ (x >> 1)) & 1;
-      __syncthreads();
-      const T* ts = tens + ((size_t)site * 4 + x) * (D * D * D * D);
-      for (int e = threadIdx.x; e < 2 * H * H; e += blockDim.x) {
-        // input pair ia = (o, h) of class ti, output pair ib = (n, h') of class ti ^ px
-        const int ti = e / (H * H), ia = (e / H) % H, ib = e % H;
-        const int o = ia / (D / 2), h = ((ti ^ (o & 1)) & 1) + 2 * (ia % (D / 2));
-        const int to = ti ^ px;
-        const int n = ib / (D / 2), hp = ((to ^ (n & 1)) & 1) + 2 * (ib % (D / 2));
-        const int u = side ? n : o, d = side ? o : n;
-        T val = ts[((h * D + u) * D + hp) * D + d];
-        if (r >= 1 && (u & 1) && ((h + nleft) & 1)) val = -val;
-        A2[e] = val;
-      }
       __syncthreads();
       for (int gi = threadIdx.x; gi < NS / D; gi += blockDim.x) {
         const int lo = gi % stride, hi = gi / stride;
@@ -321,7 +328,7 @@ __global__ void __launch_bounds__(CHI_NT)
           any |= in[ia] != T(0);
         }
         if (!any) continue;
-        const T* Ab = A2 + ti * H * H;
+        const T* Ab = A2 + (c * 2 + ti) * H * H;
         T outv[H];
 #pragma unroll
         for (int ib = 0; ib < H; ++ib) outv[ib] = T(0);
@@ -343,7 +350,6 @@ __global__ void __launch_bounds__(CHI_NT)
         }
       }
       par ^= px;
-      nleft += __popcll((up >> site) & 1ull) + __popcll((dn >> site) & 1ull);
     }
     __syncthreads();
     // rescale the state (the h != 0 slices are zero after the open right edge)
@@ -748,7 +754,7 @@ int chi_plan(int Lx, int Ly, int D, int chi, ChiSched& sc) {
 template <typename T, int D>
 int build_sides_d(const void* tens, const ChiSched& sc, const uint64_t* cfg, const int32_t* cfg_idx,
                   const uint8_t* sides, int64_t n_items, const int* count, T* state, int* ex, cudaStream_t st) {
-  const size_t smem = ChiSmem<T>::bytes(sc.NS, D);
+  const size_t smem = ChiSmem<T>::bytes(sc.NS, D, sc.Ly);
   if (cudaFuncSetAttribute(k_chi_absorb<T, D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return VMC_ERR_CUDA;
   const size_t tsm = ChiTruncSmem<T>::bytes();
