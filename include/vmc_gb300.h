@@ -396,6 +396,21 @@ int vmc_peps_chi_local_energy(int prec, const void* tensors, int Lx, int Ly, int
                               int64_t B, const int32_t* edges, double t, double U, const int32_t* pairs,
                               const int32_t* offs, const int32_t* offs_host, int64_t P, double* term, double* eloc,
                               void* work, int64_t work_rows, void* stream);
+/* vmc_peps_chi_logpsi_grad — O (B, ldo >= Lx*Ly*4*D^4, dtype of prec) = d log|psi| / d
+ *   tensors through the truncation (the reference differentiates its truncated
+ *   contraction with torch autograd, vmc_torch/GPU/vmc_utils.py:1389-1634): the
+ *   cotangent of each side's rank-chi truncation against the other side's
+ *   truncated state (first-order change of the kept singular subspace, weights
+ *   1/(s_i^2 - s_j^2) between kept and dropped directions), then a reverse row
+ *   sweep that recomputes the forward column states.  Supported when the only
+ *   truncated cut is one cut after each side's last row and its parity blocks
+ *   are at most 32 x 32 (6x6 D=4 chi in [16, 64), 4x4 D=4 chi in [4, 16)), else
+ *   VMC_ERR_UNSUPPORTED; FP64 also needs 2 * D^(Ly+1) doubles of shared memory.
+ *   work: *bytes from vmc_peps_chi_grad_work_bytes for work_rows walkers.  Rows of
+ *   zero amplitude stay zero. */
+int vmc_peps_chi_grad_work_bytes(int prec, int Lx, int Ly, int D, int chi, int64_t work_rows, int64_t* bytes);
+int vmc_peps_chi_logpsi_grad(int prec, const void* tensors, int Lx, int Ly, int D, int chi, const uint64_t* occ,
+                             int64_t B, void* O, int64_t ldo, void* work, int64_t work_rows, void* stream);
 
 /* ---- Point-group symmetry projection with fermionic signs
  * (FermionSymmetryProjectedModel, vmc_torch/GPU/models/symmetry.py:770-1136) ----

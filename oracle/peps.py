@@ -363,6 +363,55 @@ def amp_state_chi(T, x, chi, with_norms=False):
     return g * float(top @ bot)
 
 
+def logamp_grad_chi(T, x, chi):
+    """d log|psi_chi| / d T (FP64) by torch autograd through the full-state
+    chi-truncated contraction with torch.linalg.svd at every scheduled cut
+    (the reference differentiates its quimb contraction with torch autograd,
+    vmc_torch/GPU/vmc_utils.py:1389-1634, through the same truncated SVDs)."""
+    import torch
+    Lx, Ly, _, D = T.shape[:4]
+    x = np.asarray(x, dtype=np.int64).reshape(Lx, Ly)
+    Tt = torch.tensor(T, dtype=torch.float64, requires_grad=True)
+    bp = np.arange(D) % 2
+    A = [[None] * Ly for _ in range(Lx)]
+    for r in range(Lx):
+        nleft = 0
+        for c in range(Ly):
+            a = Tt[r, c, int(x[r, c])]
+            if r > 0:
+                e = (bp[None, :] * (bp[:, None] + nleft)) % 2
+                a = a * torch.tensor((1 - 2 * e)[:, :, None, None], dtype=torch.float64)
+            A[r][c] = a
+            nleft += int(S_COUNT[x[r, c]])
+    sched = chi_schedule(Lx, Ly, D, chi)
+    eye0 = torch.zeros(D, dtype=torch.float64)
+    eye0[0] = 1.0
+
+    def side(rows, top):
+        psi = torch.zeros(D ** Ly, dtype=torch.float64)
+        psi = psi.index_put((torch.tensor([0]),), torch.tensor([1.0], dtype=torch.float64))
+        for a, r in enumerate(rows):
+            W = psi.reshape((D,) * Ly)[..., None] * eye0
+            for c in range(Ly):
+                t = A[r][c] if top else A[r][c].permute(0, 3, 2, 1)
+                W = torch.movedim(W, c, -2)
+                W = torch.einsum("...oh,hopn->...np", W, t)
+                W = torch.movedim(W, -2, c)
+            psi = W[..., 0].reshape(-1)
+            for k in sched[a]:
+                M = psi.reshape(D ** k, D ** (Ly - k))
+                u, sv, vh = torch.linalg.svd(M, full_matrices=False)
+                rk = min(chi, sv.shape[0])
+                psi = ((u[:, :rk] * sv[:rk]) @ vh[:rk]).reshape(-1)
+        return psi
+
+    top = side(range(0, Lx // 2), True)
+    bot = side(range(Lx - 1, Lx // 2 - 1, -1), False)
+    z = top @ bot
+    torch.log(torch.abs(z)).backward()
+    return Tt.grad.numpy()
+
+
 def logamp(T, X, method="rows", chi=None):
     if method == "chi":
         a = np.array([amp_state_chi(T, x, chi) for x in np.asarray(X)])

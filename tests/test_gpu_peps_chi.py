@@ -119,3 +119,73 @@ def test_chi_local_energy_vs_oracle(Lx, Ly, D, chi, nup, B):
     ref = hubbard.local_energy(X, lattice.square_edges(Lx, Ly), 1.0, 8.0,
                                lambda y: np.array([peps.amp_state_chi(T, v, chi) for v in y]))
     np.testing.assert_allclose(eloc.cpu().numpy(), ref, rtol=1e-8, atol=1e-8)
+
+
+def _chi_O_oracle(T, X, chi):
+    Lx, Ly, _, D = T.shape[:4]
+    return np.stack([peps.logamp_grad_chi(T, x, chi).reshape(-1) for x in X])
+
+
+def test_chi_logpsi_grad_fp64_vs_autograd():
+    """O through the truncation against torch autograd of the oracle's
+    truncated contraction (torch.linalg.svd, as the reference differentiates
+    its quimb contraction)."""
+    Lx, Ly, D, chi = 4, 4, 4, 8
+    T = peps.init_tensors(Lx, Ly, D, seed=12)
+    X = lattice.random_initial_configs(12, Lx * Ly, 4, 4, seed=13)
+    m = _model(Lx, Ly, D, T, chi)
+    st = m.bind_state(torch.as_tensor(X, device=DEV))
+    O = m.logpsi_grad(st, work_rows=5).cpu().numpy()
+    ref = _chi_O_oracle(T, X, chi)
+    err = np.abs(O - ref).max(axis=1) / np.abs(ref).max(axis=1)
+    print("4x4 chi=8 FP64 O: max row error / max|O| = %.2e" % err.max())
+    assert err.max() < 1e-8
+    assert np.array_equal(O != 0, ref != 0) or np.abs(O[(O != 0) != (ref != 0)]).max() < 1e-12
+
+
+def test_chi_logpsi_grad_fp32_6x6():
+    Lx, Ly, D, chi = 6, 6, 4, 16
+    T = peps.init_tensors(Lx, Ly, D, seed=14)
+    X = lattice.random_initial_configs(6, Lx * Ly, 16, 16, seed=15)
+    m = _model(Lx, Ly, D, T, chi, precision="fp32")
+    st = m.bind_state(torch.as_tensor(X, device=DEV))
+    O = m.logpsi_grad(st).double().cpu().numpy()
+    ref = _chi_O_oracle(T.astype(np.float32).astype(np.float64), X, chi)
+    rel = np.linalg.norm(O - ref, axis=1) / np.linalg.norm(ref, axis=1)
+    print("6x6 chi=16 FP32 O: |dO| / |O| per walker: max %.2e median %.2e" % (rel.max(), np.median(rel)))
+    assert rel.max() < 1e-3
+
+
+def test_chi_logpsi_grad_euler_identity_at_scale():
+    """psi is homogeneous of degree 1 in every site tensor (each row enters
+    the boundary linearly and the rank-chi truncation is homogeneous), so for
+    every walker and site sum_e T_e d log|psi| / d T_e = 1: a check at the
+    benchmark's size (6x6, chi = 16, FP32, 2048 walkers)."""
+    Lx, Ly, D, chi, B = 6, 6, 4, 16, 2048
+    m = vg.FPEPS_GB300(Lx, Ly, D, max_bond=chi, generator=torch.Generator().manual_seed(5)).to(DEV)
+    fx = vg.init_walkers(B, Lx * Ly, 16, 16, seed=3, device=DEV)
+    st = m.bind_state(fx)
+    O = m.logpsi_grad(st)
+    Tf = m.params[0].detach().float().reshape(1, Lx * Ly, 4 * D ** 4)
+    per_site = (O.reshape(B, Lx * Ly, 4 * D ** 4) * Tf).sum(-1).double()
+    dev = (per_site - 1).abs()
+    print("Euler identity, 2048 walkers x 36 sites: max |sum - 1| = %.2e, median %.2e"
+          % (dev.max().item(), dev.median().item()))
+    assert torch.isfinite(O).all()
+    assert dev.median().item() < 1e-4 and dev.max().item() < 1e-2
+
+
+def test_chi_sr_steps_run():
+    """Two SR steps of the 6x6 chi = 16 model through VMC_GB300: sampling,
+    local energies, O through the truncation, minSR."""
+    Lx, Ly, B = 6, 6, 512
+    H = vg.spinful_Fermi_Hubbard_square_lattice_torch(Lx, Ly, 1.0, 8.0, 32, n_fermions_per_spin=(16, 16))
+    H.precompute_hops_gpu(DEV)
+    m = vg.FPEPS_GB300(Lx, Ly, 4, max_bond=16, generator=torch.Generator().manual_seed(2), init_std=0.5).to(DEV)
+    fx = vg.init_walkers(B, Lx * Ly, 16, 16, seed=4, device=DEV)
+    cfg = vg.VMCLoopConfig(vmc_steps=2, ns_per_rank=B, grad_batch_size=256, n_params=m.n_params, nsites=Lx * Ly,
+                           learning_rate=0.01, diag_shift=1e-3, burn_in_steps=2)
+    drv = vg.VMC_GB300(vg.MetropolisExchangeSpinfulSamplerGB300(seed=3), vg.MinSRGB300(), vg.SGDGB300(0.01))
+    hist, fx = drv.run_vmc_loop(fx, m, H, H.graph, 0, 1, cfg)
+    print("6x6 chi=16 SR energies per site:", np.round(hist, 5))
+    assert len(hist) == 2 and all(np.isfinite(hist))

@@ -83,6 +83,8 @@ SIGNATURES = {
     "vmc_peps_chi_sweep": [I32, P, I32, I32, I32, I32, P, I64, P, I32, I32, F32, U64, U64, P, P, P, P, P, P, P, P,
                            I64, P],
     "vmc_peps_chi_local_energy": [I32, P, I32, I32, I32, I32, P, I64, P, F64, F64, P, P, P, I64, P, P, P, I64, P],
+    "vmc_peps_chi_grad_work_bytes": [I32, I32, I32, I32, I32, I64, P],
+    "vmc_peps_chi_logpsi_grad": [I32, P, I32, I32, I32, I32, P, I64, P, I64, P, I64, P],
     "vmc_sym_images": [P, I64, I32, P, P, I32, P, P, P],
     "vmc_sym_combine": [P, P, P, P, I64, I32, P, P, P, P],
     "vmc_sym_grad_combine": [I32, P, I64, P, I64, I32, I64, P, I64, P],

@@ -250,6 +250,139 @@ __device__ __forceinline__ int side_parity(uint64_t up, uint64_t dn, int Lx, int
   return (__popcll(up & m) + __popcll(dn & m)) & 1;
 }
 
+// Pair ia (< D^2/2) of parity class t: (d, h) with p(d) + p(h) = t.
+template <int D>
+__device__ __forceinline__ void class_pair(int t, int ia, int& d, int& h) {
+  d = ia / (D / 2);
+  h = ((t ^ (d & 1)) & 1) + 2 * (ia % (D / 2));
+}
+
+// Signed site tensors of row r in parity blocks, all columns:
+// A2[c][ti][ia][ib] = A(r, c)[h][old][h'][new] for the input pair ia = (old, h)
+// of class ti and the output pair ib = (new, h') of class ti ^ p(x_rc).
+template <typename T, int D>
+__device__ void load_row_tables(const T* __restrict__ tens, uint64_t up, uint64_t dn, int r, int Ly, int side,
+                                T* A2) {
+  constexpr int H = D * D / 2;
+  for (int e = threadIdx.x; e < Ly * 2 * H * H; e += blockDim.x) {
+    const int c = e / (2 * H * H), el = e - c * 2 * H * H;
+    const int site = r * Ly + c;
+    const int x = site_state(up, dn, site);
+    const int px = (x ^ (x >> 1)) & 1;
+    const uint64_t lm = bits_below(site) & ~bits_below(r * Ly);
+    const int nleft = __popcll(up & lm) + __popcll(dn & lm);
+    const int ti = el / (H * H), ia = (el / H) % H, ib = el % H;
+    int o, h, n, hp;
+    class_pair<D>(ti, ia, o, h);
+    class_pair<D>(ti ^ px, ib, n, hp);
+    const int u = side ? n : o, d = side ? o : n;
+    T val = tens[((size_t)site * 4 + x) * (D * D * D * D) + ((h * D + u) * D + hp) * D + d];
+    if (r >= 1 && (u & 1) && ((h + nleft) & 1)) val = -val;
+    A2[e] = val;
+  }
+}
+
+// Tensor index (within the site's D^4 block) and sign-rule sign of entry
+// (ti, ia, ib) of a column's table; inverse of load_row_tables.
+template <int D>
+__device__ __forceinline__ int table_entry(int ti, int ia, int ib, int px, int side, int r, int nleft, int& sgn) {
+  int o, h, n, hp;
+  class_pair<D>(ti, ia, o, h);
+  class_pair<D>(ti ^ px, ib, n, hp);
+  const int u = side ? n : o, d = side ? o : n;
+  sgn = (r >= 1 && (u & 1) && ((h + nleft) & 1)) ? -1 : 1;
+  return ((h * D + u) * D + hp) * D + d;
+}
+
+// One column of a row absorption, in place on W[h][idx] (all threads).
+// par: electron parity absorbed before this column; px: the site's.
+template <typename T, int D>
+__device__ void column_forward(T* W, int NS, int stride, int par, int px, const T* Ac) {
+  constexpr int H = D * D / 2;
+  for (int gi = threadIdx.x; gi < NS / D; gi += blockDim.x) {
+    const int lo = gi % stride, hi = gi / stride;
+    const int base = hi * stride * D + lo;
+    const int ti = (par ^ digit_parity<D>((uint32_t)base)) & 1, to = ti ^ px;
+    T in[H];
+    bool any = false;
+#pragma unroll
+    for (int ia = 0; ia < H; ++ia) {
+      int o, h;
+      class_pair<D>(ti, ia, o, h);
+      in[ia] = W[h * NS + base + o * stride];
+      any |= in[ia] != T(0);
+    }
+    if (!any) continue;
+    const T* Ab = Ac + ti * H * H;
+    T outv[H];
+#pragma unroll
+    for (int ib = 0; ib < H; ++ib) outv[ib] = T(0);
+#pragma unroll
+    for (int ia = 0; ia < H; ++ia)
+#pragma unroll
+      for (int ib = 0; ib < H; ++ib) outv[ib] += in[ia] * Ab[ia * H + ib];
+    if (px) {  // the input class empties
+#pragma unroll
+      for (int ia = 0; ia < H; ++ia) {
+        int o, h;
+        class_pair<D>(ti, ia, o, h);
+        W[h * NS + base + o * stride] = T(0);
+      }
+    }
+#pragma unroll
+    for (int ib = 0; ib < H; ++ib) {
+      int n, hp;
+      class_pair<D>(to, ib, n, hp);
+      W[hp * NS + base + n * stride] = outv[ib];
+    }
+  }
+}
+
+// Transpose of column_forward on a cotangent Wb (in place): the output class
+// cotangents map back onto the input class.
+template <typename T, int D>
+__device__ void column_adjoint(T* Wb, int NS, int stride, int par, int px, const T* Ac) {
+  constexpr int H = D * D / 2;
+  for (int gi = threadIdx.x; gi < NS / D; gi += blockDim.x) {
+    const int lo = gi % stride, hi = gi / stride;
+    const int base = hi * stride * D + lo;
+    const int ti = (par ^ digit_parity<D>((uint32_t)base)) & 1, to = ti ^ px;
+    T g[H];
+    bool any = false;
+#pragma unroll
+    for (int ib = 0; ib < H; ++ib) {
+      int n, hp;
+      class_pair<D>(to, ib, n, hp);
+      g[ib] = Wb[hp * NS + base + n * stride];
+      any |= g[ib] != T(0);
+    }
+    if (!any) continue;
+    const T* Ab = Ac + ti * H * H;
+    T inb[H];
+#pragma unroll
+    for (int ia = 0; ia < H; ++ia) {
+      T acc = T(0);
+#pragma unroll
+      for (int ib = 0; ib < H; ++ib) acc += Ab[ia * H + ib] * g[ib];
+      inb[ia] = acc;
+    }
+    if (px) {
+#pragma unroll
+      for (int ib = 0; ib < H; ++ib) {
+        int n, hp;
+        class_pair<D>(to, ib, n, hp);
+        Wb[hp * NS + base + n * stride] = T(0);
+      }
+    }
+#pragma unroll
+    for (int ia = 0; ia < H; ++ia) {
+      int o, h;
+      class_pair<D>(ti, ia, o, h);
+      Wb[h * NS + base + o * stride] = inb[ia];
+    }
+  }
+}
+
 // Absorbs rows [a0, a1) of each item's side into its boundary state (slot
 // 2 ci + side of state / expo; a0 == 0 starts from the empty boundary).  One
 // CTA per item, W[h][idx] (D x NS) in shared memory.  Z2 structure: while a
@@ -258,11 +391,14 @@ __device__ __forceinline__ int side_parity(uint64_t up, uint64_t dn, int Lx, int
 // p(h') + p(n) equals the site's; so a group's D^2 inputs hold D^2/2 non-zero
 // values, mapped by a (D^2/2)^2 block of A onto the D^2/2 outputs of the
 // other class when the site's parity is odd (the emptied slots are zeroed).
+// keep / row_e (nullable): the normalised state after every row and the
+// row's power-of-two exponent, at [(slot * rows + a)], for the adjoint.
 template <typename T, int D>
 __global__ void __launch_bounds__(CHI_NT)
     k_chi_absorb(const T* __restrict__ tens, ChiSched sc, const uint64_t* __restrict__ cfg,
                  const int32_t* __restrict__ cfg_idx, const uint8_t* __restrict__ sides, int64_t n_items,
-                 const int* __restrict__ count, int a0, int a1, T* __restrict__ state, int* __restrict__ expo_io) {
+                 const int* __restrict__ count, int a0, int a1, T* __restrict__ state, int* __restrict__ expo_io,
+                 T* __restrict__ keep, int* __restrict__ row_e) {
   constexpr int H = D * D / 2;  // non-zero entries of a group
   extern __shared__ __align__(16) unsigned char smraw[];
   const int64_t item = blockIdx.x;
@@ -292,63 +428,13 @@ __global__ void __launch_bounds__(CHI_NT)
     const int r = side ? (Lx - 1 - a) : a;
     // the row's signed tensors, all columns at once (one global-load latency per row)
     __syncthreads();
-    for (int e = threadIdx.x; e < Ly * 2 * H * H; e += blockDim.x) {
-      const int c = e / (2 * H * H), el = e - c * 2 * H * H;
-      const int site = r * Ly + c;
-      const int x = site_state(up, dn, site);
-      const int px = (x ^ (x >> 1)) & 1;
-      const uint64_t lm = bits_below(site) & ~bits_below(r * Ly);
-      const int nleft = __popcll(up & lm) + __popcll(dn & lm);
-      // input pair ia = (o, h) of class ti, output pair ib = (n, h') of class ti ^ px
-      const int ti = el / (H * H), ia = (el / H) % H, ib = el % H;
-      const int o = ia / (D / 2), h = ((ti ^ (o & 1)) & 1) + 2 * (ia % (D / 2));
-      const int to = ti ^ px;
-      const int n = ib / (D / 2), hp = ((to ^ (n & 1)) & 1) + 2 * (ib % (D / 2));
-      const int u = side ? n : o, d = side ? o : n;
-      T val = tens[((size_t)site * 4 + x) * (D * D * D * D) + ((h * D + u) * D + hp) * D + d];
-      if (r >= 1 && (u & 1) && ((h + nleft) & 1)) val = -val;
-      A2[e] = val;
-    }
+    load_row_tables<T, D>(tens, up, dn, r, Ly, side, A2);
     int stride = NS / D;
     for (int c = 0; c < Ly; ++c, stride /= D) {
-      const int site = r * Ly + c;
-      const int x = site_state(up, dn, site);
+      const int x = site_state(up, dn, r * Ly + c);
       const int px = (x ^ (x >> 1)) & 1;
       __syncthreads();
-      for (int gi = threadIdx.x; gi < NS / D; gi += blockDim.x) {
-        const int lo = gi % stride, hi = gi / stride;
-        const int base = hi * stride * D + lo;
-        const int ti = (par ^ digit_parity<D>((uint32_t)base)) & 1, to = ti ^ px;
-        T in[H];
-        bool any = false;
-#pragma unroll
-        for (int ia = 0; ia < H; ++ia) {
-          const int o = ia / (D / 2), h = ((ti ^ (o & 1)) & 1) + 2 * (ia % (D / 2));
-          in[ia] = W[h * NS + base + o * stride];
-          any |= in[ia] != T(0);
-        }
-        if (!any) continue;
-        const T* Ab = A2 + (c * 2 + ti) * H * H;
-        T outv[H];
-#pragma unroll
-        for (int ib = 0; ib < H; ++ib) outv[ib] = T(0);
-#pragma unroll
-        for (int ia = 0; ia < H; ++ia)
-#pragma unroll
-          for (int ib = 0; ib < H; ++ib) outv[ib] += in[ia] * Ab[ia * H + ib];
-        if (px) {  // the input class empties
-#pragma unroll
-          for (int ia = 0; ia < H; ++ia) {
-            const int o = ia / (D / 2), h = ((ti ^ (o & 1)) & 1) + 2 * (ia % (D / 2));
-            W[h * NS + base + o * stride] = T(0);
-          }
-        }
-#pragma unroll
-        for (int ib = 0; ib < H; ++ib) {
-          const int n = ib / (D / 2), hp = ((to ^ (n & 1)) & 1) + 2 * (ib % (D / 2));
-          W[hp * NS + base + n * stride] = outv[ib];
-        }
-      }
+      column_forward<T, D>(W, NS, stride, par, px, A2 + c * 2 * H * H);
       par ^= px;
     }
     __syncthreads();
@@ -367,6 +453,12 @@ __global__ void __launch_bounds__(CHI_NT)
     expo += e2;
     __syncthreads();
     for (int e = threadIdx.x; e < NS; e += blockDim.x) W[e] = scalbn(W[e], -e2);
+    if (keep) {
+      __syncthreads();
+      T* kp = keep + (slot * sc.rows + a) * (int64_t)NS;
+      for (int e = threadIdx.x; e < NS; e += blockDim.x) kp[e] = W[e];
+      if (threadIdx.x == 0) row_e[slot * sc.rows + a] = e2;
+    }
   }
   __syncthreads();
   for (int e = threadIdx.x; e < NS; e += blockDim.x) st[e] = (zero || bad) ? T(0) : W[e];
@@ -719,6 +811,265 @@ __global__ void k_chi_eloc_reduce(int64_t B, const uint64_t* __restrict__ occ, c
   eloc[w] = s;
 }
 
+// ---------------------------------------------------------------------------
+// Log-derivatives through the truncation (schedules whose only truncated cut
+// is one cut after each side's last row, with parity blocks that fit a warp:
+// 6x6 D=4 chi in [16, 64), 4x4 D=4 chi in [4, 16)).  With z = <P(phi_t),
+// beta_b> in the normalised units of the states (phi_t the top state before
+// its truncation P, beta_b the truncated bottom state):
+//   dz = <dphi_t, cot_t>,  cot_t = (dP at phi_t)^T beta_b,
+// and d log|psi| / dA(r, c) = <d phi_t / dA(r, c), cot_t> / z, the hole
+// contraction of the side's rows against cot_t (likewise for the bottom).
+// The cotangent of the rank-k truncation of M = sum_i s_i q_i v_i^T (q, v
+// singular vectors, u_i = s_i v_i the one-sided Jacobi rows) against B is
+//   Mbar = P_k B + sum_{i kept, j dropped} w_ij (q_j u_i^T + q_i u_j^T),
+//   w_ij = (q_j^T B u_i + q_i^T B u_j) / (s_i^2 - s_j^2),
+// the first-order change of the kept subspace (it couples kept and dropped
+// directions only, and only within a parity block).
+// ---------------------------------------------------------------------------
+template <typename T>
+struct ChiAdj {
+  static constexpr int ITEMS = sizeof(T) == 4 ? 4 : 2;  // items per CTA (two warps each)
+  static constexpr int PER_ITEM = 2 * 4 * 32 * 33 + 64;  // T elements: per block Q, U, B/X, C/R; lam
+  static size_t bytes() { return (size_t)ITEMS * (PER_ITEM * sizeof(T) + 64 * sizeof(int)); }
+};
+
+template <typename T, int D>
+__global__ void __launch_bounds__(64 * ChiAdj<T>::ITEMS)
+    k_chi_trunc_adj(ChiSched sc, int k, const uint64_t* __restrict__ cfg, int64_t n_items,
+                    const T* __restrict__ phi_keep, const T* __restrict__ trunc_state, const int* __restrict__ ex,
+                    T* __restrict__ cot) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int warp = threadIdx.x >> 5, ln = threadIdx.x & 31;
+  const int il = warp >> 1, b = warp & 1;
+  const int64_t item = (int64_t)blockIdx.x * ChiAdj<T>::ITEMS + il;
+  const bool live = item < n_items;
+  T* base_s = reinterpret_cast<T*>(smraw) + (size_t)il * ChiAdj<T>::PER_ITEM;
+  T* Qs = base_s + (b * 4 + 0) * 32 * 33;
+  T* Us = base_s + (b * 4 + 1) * 32 * 33;
+  T* BX = base_s + (b * 4 + 2) * 32 * 33;
+  T* CR = base_s + (b * 4 + 3) * 32 * 33;
+  T* lam = base_s + 8 * 32 * 33;  // [2][32]
+  int* keep = reinterpret_cast<int*>(reinterpret_cast<T*>(smraw) + (size_t)ChiAdj<T>::ITEMS * ChiAdj<T>::PER_ITEM) +
+              il * 64;
+  const int NS = sc.NS;
+  int nL = 1;
+  for (int i = 0; i < k; ++i) nL *= D;
+  const int nR = NS / nL;
+  const bool left = nL <= nR;
+  const int n = left ? nL : nR, nb = n >> 1, nq = (NS / n) >> 1;
+  bool on = false;
+  int qcls = 0;
+  const T* phi = nullptr;
+  const T* bst = nullptr;
+  if (live) {
+    const int64_t ci = item >> 1;
+    const int side = (int)(item & 1);
+    on = ex[item] != CHI_EXP_ZERO && ex[item] != CHI_EXP_BAD && ex[item ^ 1] != CHI_EXP_ZERO &&
+         ex[item ^ 1] != CHI_EXP_BAD;
+    phi = phi_keep + (item * sc.rows + sc.rows - 1) * (int64_t)NS;
+    bst = trunc_state + (item ^ 1) * (int64_t)NS;
+    qcls = side_parity(cfg[2 * ci], cfg[2 * ci + 1], sc.Lx, sc.Ly, side, sc.rows) ^ b;
+  }
+  const uint32_t pi = block_member<D>(b, ln);
+  auto at = [&](uint32_t p, uint32_t q) -> int64_t {
+    return left ? (int64_t)p * nR + q : (int64_t)q * nR + p;
+  };
+  T u[32];
+#pragma unroll
+  for (int j = 0; j < 32; ++j) u[j] = (on && ln < nb && j < nq) ? phi[at(pi, block_member<D>(qcls, j))] : T(0);
+  warp_hestenes<T>(u, Qs, lam + b * 32);
+#pragma unroll
+  for (int j = 0; j < 32; ++j) {
+    Us[ln * 33 + j] = u[j];
+    BX[ln * 33 + j] = (on && ln < nb && j < nq) ? bst[at(pi, block_member<D>(qcls, j))] : T(0);
+  }
+  __syncthreads();
+  {
+    const T l = lam[b * 32 + ln];
+    int rank = 0;
+    for (int e = 0; e < 64; ++e) {
+      const int b2 = e >> 5, i2 = e & 31;
+      if (i2 >= nb) continue;
+      const T l2 = lam[e];
+      rank += (l2 > l) || (l2 == l && (b2 < b || (b2 == b && i2 < ln)));
+    }
+    keep[b * 32 + ln] = (ln < nb) && rank < sc.chi;
+  }
+  __syncthreads();
+  // C = Q B (lane a: row a)
+  T crow[32];
+  {
+    T qrow[32];
+#pragma unroll
+    for (int p = 0; p < 32; ++p) qrow[p] = Qs[ln * 33 + p];
+#pragma unroll
+    for (int q = 0; q < 32; ++q) {
+      T acc = T(0);
+#pragma unroll
+      for (int p = 0; p < 32; ++p) acc = fma(qrow[p], BX[p * 33 + q], acc);
+      crow[q] = acc;
+    }
+  }
+  __syncwarp();
+  // X[a][c] = q_a^T B u_c, into BX
+#pragma unroll
+  for (int c = 0; c < 32; ++c) {
+    T acc = T(0);
+#pragma unroll
+    for (int q = 0; q < 32; ++q) acc = fma(crow[q], Us[c * 33 + q], acc);
+    BX[ln * 33 + c] = acc;
+  }
+  __syncwarp();
+  // R[a][:] = keep_a C[a][:] + sum over mixed pairs (a, c) of w * u_c
+  {
+    const bool ka = keep[b * 32 + ln] != 0;
+    const T la = lam[b * 32 + ln];
+    T r[32];
+#pragma unroll
+    for (int q = 0; q < 32; ++q) r[q] = ka ? crow[q] : T(0);
+    for (int c = 0; c < nb; ++c) {
+      const bool kc = keep[b * 32 + c] != 0;
+      if (ka == kc || ln >= nb) continue;
+      const T den = ka ? (la - lam[b * 32 + c]) : (lam[b * 32 + c] - la);
+      const T w = (BX[ln * 33 + c] + BX[c * 33 + ln]) / den;
+#pragma unroll
+      for (int q = 0; q < 32; ++q) r[q] = fma(w, Us[c * 33 + q], r[q]);
+    }
+#pragma unroll
+    for (int q = 0; q < 32; ++q) CR[ln * 33 + q] = r[q];
+  }
+  __syncwarp();
+  // Mbar = Q^T R: lane p writes row p of the block
+  if (on && ln < nb) {
+    T* ct = cot + item * (int64_t)NS;
+    for (int q = 0; q < nq; ++q) {
+      T acc = T(0);
+#pragma unroll
+      for (int a = 0; a < 32; ++a) acc = fma(Qs[a * 33 + ln], CR[a * 33 + q], acc);
+      ct[at(pi, block_member<D>(qcls, q))] = acc;
+    }
+  }
+}
+
+// z[w] = <top, bottom> of the normalised truncated states (FP64), 0 when a side vanished.
+template <typename T>
+__global__ void k_chi_zdot(const T* __restrict__ st, const int* __restrict__ ex, int NS, int64_t R,
+                           double* __restrict__ z) {
+  const int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (w >= R) return;
+  const double v = warp_dot(st + 2 * w * NS, st + (2 * w + 1) * NS, NS);
+  if ((threadIdx.x & 31) == 0) {
+    const bool dead = ex[2 * w] == CHI_EXP_ZERO || ex[2 * w] == CHI_EXP_BAD || ex[2 * w + 1] == CHI_EXP_ZERO ||
+                      ex[2 * w + 1] == CHI_EXP_BAD;
+    z[w] = dead ? 0.0 : v;
+  }
+}
+
+// Reverse row sweep of one side (item = 2 w + side): the cotangent of the
+// side's final state goes back through its rows (each row's exponent scales
+// it), column by column; the forward state before a column is recomputed from
+// the row's stored input state.  Per column the site's gradient is
+// sum over groups of (input entry) x (output cotangent), written to O with the
+// sign rule's sign and divided by z.  W and the cotangent Wb in shared memory.
+template <typename T, int D>
+__global__ void __launch_bounds__(CHI_NT)
+    k_chi_grad_side(const T* __restrict__ tens, ChiSched sc, const uint64_t* __restrict__ cfg, int64_t n_items,
+                    const T* __restrict__ keep, const int* __restrict__ row_e, const T* __restrict__ cot,
+                    const double* __restrict__ z, T* __restrict__ O, int64_t ldo) {
+  constexpr int H = D * D / 2, NE = 2 * H * H;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int64_t item = blockIdx.x;
+  if (item >= n_items) return;
+  const int NS = sc.NS, Ly = sc.Ly, Lx = sc.Lx;
+  T* W = reinterpret_cast<T*>(smraw);
+  T* Wb = W + (size_t)D * NS;
+  T* A2 = Wb + (size_t)D * NS;
+  T* part = A2 + (size_t)Ly * NE;   // [CHI_NT / NE][NE]
+  T* red = part + CHI_NT;
+  const int64_t w = item >> 1;
+  const int side = (int)(item & 1);
+  const uint64_t up = cfg[2 * w], dn = cfg[2 * w + 1];
+  const double zw = z[w];
+  if (zw == 0.0 || !isfinite(zw)) return;
+  T* Ow = O + w * ldo;
+  for (int e = threadIdx.x; e < D * NS; e += blockDim.x) Wb[e] = (e < NS) ? cot[item * (int64_t)NS + e] : T(0);
+  int fexp = 0;  // the cotangent is Wb * 2^fexp
+  const int halves = CHI_NT / NE;
+  for (int a = sc.rows - 1; a >= 0; --a) {
+    const int r = side ? (Lx - 1 - a) : a;
+    fexp -= row_e[item * sc.rows + a];
+    __syncthreads();
+    load_row_tables<T, D>(tens, up, dn, r, Ly, side, A2);
+    const int par0 = side_parity(up, dn, Lx, Ly, side, a);
+    const T* in_state = a > 0 ? keep + (item * sc.rows + a - 1) * (int64_t)NS : nullptr;
+    for (int c = Ly - 1; c >= 0; --c) {
+      // forward state before column c
+      __syncthreads();
+      for (int e = threadIdx.x; e < D * NS; e += blockDim.x)
+        W[e] = (e < NS) ? (in_state ? in_state[e] : (e == 0 ? T(1) : T(0))) : T(0);
+      int par = par0, stride = NS / D;
+      for (int c2 = 0; c2 < c; ++c2, stride /= D) {
+        const int x2 = site_state(up, dn, r * Ly + c2);
+        const int px2 = (x2 ^ (x2 >> 1)) & 1;
+        __syncthreads();
+        column_forward<T, D>(W, NS, stride, par, px2, A2 + c2 * NE);
+        par ^= px2;
+      }
+      __syncthreads();
+      const int site = r * Ly + c;
+      const int x = site_state(up, dn, site);
+      const int px = (x ^ (x >> 1)) & 1;
+      // gradient of the site's table: thread (half, e), e = (ti, ia, ib)
+      {
+        const int e = threadIdx.x % NE, hf = threadIdx.x / NE;
+        const int ti = e / (H * H), ia = (e / H) % H, ib = e % H;
+        int o, h, nn, hp;
+        class_pair<D>(ti, ia, o, h);
+        class_pair<D>(ti ^ px, ib, nn, hp);
+        T acc = T(0);
+        if (hf < halves)
+          for (int gi = hf; gi < NS / D; gi += halves) {
+            const int lo = gi % stride, hi = gi / stride;
+            const int base = hi * stride * D + lo;
+            if (((par ^ digit_parity<D>((uint32_t)base)) & 1) != ti) continue;
+            acc = fma(W[h * NS + base + o * stride], Wb[hp * NS + base + nn * stride], acc);
+          }
+        part[threadIdx.x] = acc;
+      }
+      __syncthreads();
+      if (threadIdx.x < NE) {
+        T tot = T(0);
+        for (int hf = 0; hf < halves; ++hf) tot += part[hf * NE + threadIdx.x];
+        const int e = threadIdx.x, ti = e / (H * H), ia = (e / H) % H, ib = e % H;
+        const uint64_t lm = bits_below(site) & ~bits_below(r * Ly);
+        const int nleft = __popcll(up & lm) + __popcll(dn & lm);
+        int sgn;
+        const int idx = table_entry<D>(ti, ia, ib, px, side, r, nleft, sgn);
+        const double g = (double)sgn * ldexp((double)tot, fexp) / zw;
+        Ow[((int64_t)site * 4 + x) * (D * D * D * D) + idx] = (T)g;
+      }
+      __syncthreads();
+      column_adjoint<T, D>(Wb, NS, stride, par, px, A2 + c * NE);
+    }
+    __syncthreads();
+    // the cotangent of the row's input state: slice h = 0; renormalise by a power of two
+    T m = T(0);
+    for (int e = threadIdx.x; e < D * NS; e += blockDim.x) {
+      if (e >= NS) Wb[e] = T(0);
+      else m = fmax(m, fabs(Wb[e]));
+    }
+    m = cta_absmax<T>(m, red);
+    if (m > T(0) && m < T(INFINITY)) {
+      const int e2 = (int)ilogb(m);
+      fexp += e2;
+      __syncthreads();
+      for (int e = threadIdx.x; e < NS; e += blockDim.x) Wb[e] = scalbn(Wb[e], -e2);
+    }
+  }
+}
+
+
 int chi_plan(int Lx, int Ly, int D, int chi, ChiSched& sc) {
   if (Lx < 2 || (Lx & 1) || Ly < 1 || Lx * Ly > 64 || (D != 2 && D != 4) || chi < 1) return VMC_ERR_UNSUPPORTED;
   int64_t NS = 1;
@@ -753,7 +1104,8 @@ int chi_plan(int Lx, int Ly, int D, int chi, ChiSched& sc) {
 
 template <typename T, int D>
 int build_sides_d(const void* tens, const ChiSched& sc, const uint64_t* cfg, const int32_t* cfg_idx,
-                  const uint8_t* sides, int64_t n_items, const int* count, T* state, int* ex, cudaStream_t st) {
+                  const uint8_t* sides, int64_t n_items, const int* count, T* state, int* ex, cudaStream_t st,
+                  T* keep = nullptr, int* row_e = nullptr) {
   const size_t smem = ChiSmem<T>::bytes(sc.NS, D, sc.Ly);
   if (cudaFuncSetAttribute(k_chi_absorb<T, D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return VMC_ERR_CUDA;
@@ -765,7 +1117,7 @@ int build_sides_d(const void* tens, const ChiSched& sc, const uint64_t* cfg, con
     int a1 = a + 1;
     while (a1 < sc.rows && sc.cuts[a1 - 1] == 0) ++a1;
     k_chi_absorb<T, D><<<(unsigned)n_items, CHI_NT, smem, st>>>((const T*)tens, sc, cfg, cfg_idx, sides, n_items,
-                                                                count, a, a1, state, ex);
+                                                                count, a, a1, state, ex, keep, row_e);
     VMC_CUDA_CHECK_LAUNCH();
     for (int k = sc.Ly - 1; k >= 1; --k)
       if ((sc.cuts[a1 - 1] >> k) & 1u) {
@@ -896,6 +1248,71 @@ int chi_local_energy(const void* tens, const ChiSched& sc, const uint64_t* occ, 
   return VMC_OK;
 }
 
+
+// Truncation schedules the adjoint supports: one truncated cut, after each
+// side's last row, whose parity blocks fit a warp.  Returns that cut or 0.
+int chi_grad_cut(const ChiSched& sc) {
+  for (int a = 0; a + 1 < sc.rows; ++a)
+    if (sc.cuts[a]) return 0;
+  const uint32_t m = sc.cuts[sc.rows - 1];
+  if (!m || (m & (m - 1))) return 0;
+  int k = 0;
+  while (!((m >> k) & 1u)) ++k;
+  int nL = 1;
+  for (int i = 0; i < k; ++i) nL *= sc.D;
+  const int n = nL <= sc.NS / nL ? nL : sc.NS / nL;
+  return (sc.NS / n) / 2 <= 32 ? k : 0;
+}
+
+template <typename T>
+size_t chi_grad_smem(const ChiSched& sc) {
+  const int H = sc.D * sc.D / 2;
+  return ((size_t)2 * sc.D * sc.NS + (size_t)sc.Ly * 2 * H * H + CHI_NT + 32) * sizeof(T) + 16;
+}
+
+template <typename T>
+int64_t chi_grad_bytes(const ChiSched& sc, int64_t rows) {
+  return rows * (2 * ((int64_t)sc.rows + 2) * sc.NS * (int64_t)sizeof(T) + 2 * 4 + 2 * (int64_t)sc.rows * 4 + 8) +
+         8 * 256;
+}
+
+template <typename T, int D>
+int chi_logpsi_grad_d(const void* tens, const ChiSched& sc, int k, const uint64_t* occ, int64_t B, T* O, int64_t ldo,
+                      void* work, int64_t work_rows, cudaStream_t st) {
+  const size_t gsm = chi_grad_smem<T>(sc), asm_ = ChiAdj<T>::bytes();
+  if (gsm > 227 * 1024) return VMC_ERR_UNSUPPORTED;
+  if (cudaFuncSetAttribute(k_chi_grad_side<T, D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gsm) !=
+          cudaSuccess ||
+      cudaFuncSetAttribute(k_chi_trunc_adj<T, D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)asm_) !=
+          cudaSuccess)
+    return VMC_ERR_CUDA;
+  char* p = (char*)work;
+  auto take = [&](int64_t nbytes) { char* q = p; p += (nbytes + 255) & ~int64_t(255); return q; };
+  T* keep = (T*)take(2 * work_rows * sc.rows * (int64_t)sc.NS * (int64_t)sizeof(T));
+  T* state = (T*)take(2 * work_rows * (int64_t)sc.NS * (int64_t)sizeof(T));
+  T* cot = (T*)take(2 * work_rows * (int64_t)sc.NS * (int64_t)sizeof(T));
+  int* ex = (int*)take(2 * work_rows * 4);
+  int* row_e = (int*)take(2 * work_rows * sc.rows * 4);
+  double* z = (double*)take(work_rows * 8);
+  for (int64_t w0 = 0; w0 < B; w0 += work_rows) {
+    const int64_t n = (B - w0) < work_rows ? (B - w0) : work_rows;
+    const uint64_t* cfg = occ + 2 * w0;
+    if (cudaMemsetAsync(cot, 0, 2 * n * (size_t)sc.NS * sizeof(T), st) != cudaSuccess) return VMC_ERR_CUDA;
+    int rc = build_sides_d<T, D>(tens, sc, cfg, nullptr, nullptr, 2 * n, nullptr, state, ex, st, keep, row_e);
+    if (rc) return rc;
+    k_chi_zdot<T><<<(unsigned)((n + 7) / 8), 256, 0, st>>>(state, ex, sc.NS, n, z);
+    VMC_CUDA_CHECK_LAUNCH();
+    const int per = ChiAdj<T>::ITEMS;
+    k_chi_trunc_adj<T, D><<<(unsigned)((2 * n + per - 1) / per), 64 * per, asm_, st>>>(sc, k, cfg, 2 * n, keep,
+                                                                                      state, ex, cot);
+    VMC_CUDA_CHECK_LAUNCH();
+    k_chi_grad_side<T, D><<<(unsigned)(2 * n), CHI_NT, gsm, st>>>((const T*)tens, sc, cfg, 2 * n, keep, row_e, cot,
+                                                                  z, O + w0 * ldo, ldo);
+    VMC_CUDA_CHECK_LAUNCH();
+  }
+  return VMC_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -973,6 +1390,38 @@ int vmc_peps_chi_local_energy(int prec, const void* tensors, int Lx, int Ly, int
                                              work, work_rows, st)
                    : chi_local_energy<double>(tensors, sc, occ, B, edges, t, U, pairs, offs, offs_host, term, eloc,
                                               work, work_rows, st);
+}
+
+int vmc_peps_chi_grad_work_bytes(int prec, int Lx, int Ly, int D, int chi, int64_t work_rows, int64_t* bytes) {
+  ChiSched sc;
+  if ((prec != 0 && prec != 1) || work_rows <= 0 || !bytes) return VMC_ERR_ARGS;
+  int rc = chi_plan(Lx, Ly, D, chi, sc);
+  if (rc) return rc;
+  if (!chi_grad_cut(sc)) return VMC_ERR_UNSUPPORTED;
+  *bytes = prec == 0 ? chi_grad_bytes<float>(sc, work_rows) : chi_grad_bytes<double>(sc, work_rows);
+  return VMC_OK;
+}
+
+int vmc_peps_chi_logpsi_grad(int prec, const void* tensors, int Lx, int Ly, int D, int chi, const uint64_t* occ,
+                             int64_t B, void* O, int64_t ldo, void* work, int64_t work_rows, void* stream) {
+  ChiSched sc;
+  if (prec != 0 && prec != 1) return VMC_ERR_ARGS;
+  int rc = chi_plan(Lx, Ly, D, chi, sc);
+  if (rc) return rc;
+  const int k = chi_grad_cut(sc);
+  if (!k) return VMC_ERR_UNSUPPORTED;
+  const int64_t np = (int64_t)Lx * Ly * 4 * D * D * D * D;
+  if (B < 0 || ldo < np || work_rows <= 0) return VMC_ERR_ARGS;
+  if (B == 0) return VMC_OK;
+  if (!tensors || !occ || !O || !work) return VMC_ERR_ARGS;
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t es = prec == 0 ? sizeof(float) : sizeof(double);
+  if (cudaMemset2DAsync(O, (size_t)ldo * es, 0, (size_t)np * es, (size_t)B, st) != cudaSuccess) return VMC_ERR_CUDA;
+  if (prec == 0)
+    return D == 4 ? chi_logpsi_grad_d<float, 4>(tensors, sc, k, occ, B, (float*)O, ldo, work, work_rows, st)
+                  : chi_logpsi_grad_d<float, 2>(tensors, sc, k, occ, B, (float*)O, ldo, work, work_rows, st);
+  return D == 4 ? chi_logpsi_grad_d<double, 4>(tensors, sc, k, occ, B, (double*)O, ldo, work, work_rows, st)
+                : chi_logpsi_grad_d<double, 2>(tensors, sc, k, occ, B, (double*)O, ldo, work, work_rows, st);
 }
 
 }  // extern "C"

@@ -778,11 +778,27 @@ class FPEPS_GB300(WavefunctionModel_GB300):
     def logpsi_grad(self, st, out=None, work_rows=None):
         """O (B, n_params) = d log|psi| / d tensors (flattened parameter order),
         FP32 for precision "fp32", FP64 for "fp64"; hand-written reverse
-        column sweep (vmc_peps_logpsi_grad)."""
-        if self.truncated:
-            raise NotImplementedError("log-derivatives through the chi-truncated boundary contraction are not "
-                                      "implemented; use max_bond >= D**(Lx//2) (exact contraction) for SR")
+        column sweep (vmc_peps_logpsi_grad), or for a truncated model the
+        truncation's cotangent and a reverse row sweep
+        (vmc_peps_chi_logpsi_grad)."""
         T = self._tensors(st.device)
+        if self.truncated:
+            dt = torch.float32 if self._prec == 0 else torch.float64
+            if out is None:
+                out = torch.empty((st.B, self.n_params), dtype=dt, device=st.device)
+            rows = int(work_rows or min(st.B, 2048))
+            nbytes = ctypes.c_int64(0)
+            status = _lib.call_status("vmc_peps_chi_grad_work_bytes", self._prec, self.Lx, self.Ly, self.D, self.chi,
+                                      rows, ctypes.byref(nbytes), allow=(_lib.VMC_ERR_UNSUPPORTED,))
+            if status != _lib.VMC_OK:
+                raise NotImplementedError(
+                    "log-derivatives through this truncation schedule are not built (%s): they need one truncated "
+                    "cut after each side's last row with parity blocks of at most 32 x 32" % self.chi_cuts)
+            work = torch.empty(nbytes.value, dtype=torch.uint8, device=st.device)
+            _lib.call("vmc_peps_chi_logpsi_grad", self._prec, _lib.ptr(T), *self._shape_args(), self.chi,
+                      _lib.ptr(st.occ), st.B, _lib.ptr(out), out.stride(0), _lib.ptr(work), rows,
+                      _lib.stream_of(st.device))
+            return out
         dt = torch.float32 if self._prec == 0 else torch.float64
         if out is None:
             out = torch.empty((st.B, self.n_params), dtype=dt, device=st.device)
