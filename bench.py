@@ -383,7 +383,7 @@ def peps_block(dev, steps, fp32_peak_tflops, cpu=True, env_reuse=True):
 
 
 # ---------------------------------------------------------------------------
-def ess_block(dev, n_walkers, samples=192, discard=32, moves=14, sr_steps=20, pre_walkers=4096, every=10, epochs=1,
+def ess_block(dev, n_walkers, samples=192, discard=32, moves=14, sr_steps=20, pre_walkers=4096, every=10, epochs=4,
               lr=0.02, burn=120):
     """ESS/s of E_loc for plain exchange/hop Metropolis (one 112-edge sweep per
     sample) vs the learned proposal (``moves`` MH moves per sample) on the 8x8
