@@ -559,11 +559,26 @@ def sr_block(model, H, fxs, dev, fp32_peak_tflops, diag_shift=1e-4):
     if "cholesky" in stages:
         stages["cholesky"]["frac_of_fp64_nominal"] = stages["cholesky"]["tflops"] / 1.25
     o_bytes = Ns * (Nd + Ng + Nh) * F.dense.element_size()
+    # the same solve with the Gram blocks on the tensor cores (fixed-point digit split, exact leading sums)
+    tsolver = vg.MinSRGB300(record_stages=True, gram="tensor")
+    tsolver.solve(local_o=F, local_energies=E, energy_mean=float(E.mean()), total_samples=Ns,
+                  n_params=model.n_params, diag_shift=diag_shift, device=dev, run_sr=True)   # warm-up
+    (dpt, _, tinfo), tsr_ms = timed(lambda: tsolver.solve(local_o=F, local_energies=E, energy_mean=float(E.mean()),
+                                                          total_samples=Ns, n_params=model.n_params,
+                                                          diag_shift=diag_shift, device=dev, run_sr=True))
+    tstages = {}
+    for k, ms in (tsolver.last_stages or {}).items():
+        d = {"ms": ms}
+        if k in fl:
+            d["tflops"] = fl[k] / (ms / 1e3) / 1e12
+        tstages[k] = d
+    tensor = {"minsr_ms": tsr_ms, "minsr_stages": tstages, "info": tinfo,
+              "dp_rel_diff_vs_cuda_gram": float((dpt - dp).norm().item() / dp.norm().item())}
     return {"workload": "8x8 NNBF, %d walkers: per-sample O (FP32, dense %d + Kronecker %d x %d), E_loc, minSR "
                         "over %d parameters (diag shift %g)" % (Ns, Nd, Ng, Nh, model.n_params, diag_shift),
             "logpsi_grad_ms": grad_ms, "first_full_size_call": first, "O_bytes_written": o_bytes,
             "O_write_gbs": o_bytes / (grad_ms / 1e3) / 1e9, "local_energy_ms": eloc_ms, "minsr_ms": sr_ms,
-            "minsr_stages": stages, "info": info, "dp_norm": float(dp.norm().item()),
+            "minsr_stages": stages, "info": info, "dp_norm": float(dp.norm().item()), "tensor_gram": tensor,
             "peaks": "FP32 nominal %.1f TFLOP/s (152 SM x 128 lanes x 2 x max SM clock), FP64 nominal 1.25 TFLOP/s"
                      % fp32_peak_tflops}
 

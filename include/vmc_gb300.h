@@ -276,19 +276,24 @@ int vmc_sr_gram(const void* Oc, int dtype, int64_t Ns, int64_t Np, int64_t ldc, 
 int vmc_sr_cholesky(double* T, int64_t n, int64_t ldt, int* d_info, void* stream);
 /* Tensor-core Gram for FP32 inputs (no reference counterpart as an operator:
  * the reference forms lpg_scaled @ lpg_scaled.T in FP64, vmc_torch/GPU/optimizer.py:551-553).
- * vmc_split_bf16x3: X (rows, K, ld ldx) FP32 -> three BF16 planes hi, mid, lo
- *   (x = hi + mid + lo to 2^-24), each (rows_pad, kp) row-major, rows_pad a
- *   multiple of 128 >= rows, kp a multiple of 64 >= K, padding zeroed; planes
- *   holds 3 * rows_pad * kp bf16.
+ * vmc_split_bf16x3: X (rows, K, ld ldx) FP32 -> row_exp (rows_pad ints, device):
+ *   E_r with max |X[r]| < 2^E_r, and three BF16 planes hi, mid, lo holding the
+ *   7-bit integer digits of x 2^-E_r times 2^-6, 2^-13, 2^-20 (to 2^-21 of the
+ *   row's largest entry), each (rows_pad, kp) row-major, rows_pad a multiple
+ *   of 128 >= rows, kp a multiple of 64 >= K, padding zeroed; planes holds
+ *   3 * rows_pad * kp bf16.
  * vmc_sr_gram_tc: T (ns, ns, FP64, ld ldt) = [T +] alpha (X X^T) o D [+ shift I]
  *   with D (nullable, ld ldt) elementwise and `accumulate` selecting "+=";
- *   six BF16 products per element pair on tcgen05 with FP32 accumulation,
- *   drained into FP64 every 2048 columns; the full symmetric T is written.
+ *   all nine digit products per element pair on tcgen05: the leading one summed
+ *   exactly in FP32 (integer multiples of 2^-12, < 2^23 units per 2048
+ *   columns), the others in a second FP32 accumulator; drained into FP64 every
+ *   2048 columns and scaled by 2^(E_i + E_j); the full symmetric T is written.
  *   d_err (device int) receives VMC_ERR_TIMEOUT if a bounded wait gave up. */
 int vmc_split_bf16x3(const float* X, int64_t rows, int64_t K, int64_t ldx, void* planes, int64_t rows_pad,
-                     int64_t kp, void* stream);
-int vmc_sr_gram_tc(const void* planes, int64_t ns, int64_t rows_pad, int64_t kp, double alpha, double* T,
-                   int64_t ldt, const double* D, double diag_shift, int accumulate, int* d_err, void* stream);
+                     int64_t kp, int* row_exp, void* stream);
+int vmc_sr_gram_tc(const void* planes, const int* row_exp, int64_t ns, int64_t rows_pad, int64_t kp, double alpha,
+                   double* T, int64_t ldt, const double* D, double diag_shift, int accumulate, int* d_err,
+                   void* stream);
 int vmc_sr_cholesky_solve(const double* L, int64_t n, int64_t ldt, double* b, void* stream);
 int vmc_sr_rhs(const double* E, int64_t Ns, double Ebar, double* b, void* stream);
 int vmc_sr_update(const void* Oc, int dtype, int64_t Ns, int64_t Np, int64_t ldc, const double* x, double* dp,

@@ -68,13 +68,34 @@ def test_factored_minsr_mixed_precision_vs_fp64():
     assert info == 0 and r < 2e-3
 
 
+def test_tensor_core_gram_is_exact_on_digit_representable_rows():
+    """Rows whose entries are 7-bit integers times 2^-6 times a power of two
+    per row are represented exactly by the fixed-point split (one non-zero
+    digit), and the leading products are then summed exactly in FP32 and
+    FP64: the tensor-core Gram equals the FP64 Gram bit for bit."""
+    from vmc_torch_gb300 import _lib
+    Ns, K = 300, 5000
+    g = torch.Generator().manual_seed(1)
+    ints = torch.randint(-64, 65, (Ns, K), generator=g).double()
+    ints[:, 0] = 64.0                               # row max exactly 1 after scaling: E_i fixed
+    scale = torch.pow(2.0, torch.randint(-8, 9, (Ns, 1), generator=g).double())
+    Xd = ints * 2.0 ** -6 * scale * 0.5             # max |x| = 2^(e-1): E_i = e
+    X = Xd.float().to(DEV)
+    T = torch.empty((Ns, Ns), dtype=torch.float64, device=DEV)
+    solver = vg.MinSRGB300(gram="tensor")
+    solver._tc_gram(X, T, 1.0, None, 0.0, 0, DEV)
+    solver._check_tc()
+    ref = (Xd @ Xd.t()).to(DEV)
+    assert torch.equal(T, ref)
+
+
 @pytest.mark.parametrize("Ns,K", [(700, 3000), (256, 115200 // 16)])
 def test_tensor_core_gram_matches_compensated_fp32(Ns, K):
-    """vmc_sr_gram_tc (BF16 three-way split, six products on tcgen05, FP32
-    partial sums over 2048 columns drained into FP64) against the CUDA-core
-    Gram with double-float accumulation (FP64-level) on the same FP32 matrix:
-    entries within 1e-5 of the largest diagonal entry (FP32 rounding of the
-    partial sums of up to 768 tensor-core steps per chunk), also with the
+    """vmc_sr_gram_tc (fixed-point 7-bit digits under a per-row exponent, nine
+    products on tcgen05, the leading one summed exactly, drained into FP64)
+    against the CUDA-core Gram with double-float accumulation (FP64-level) on
+    the same FP32 matrix: entries within 2e-6 of the largest diagonal entry
+    (the digits round each row to 2^-20 of its largest entry), also with the
     elementwise factor D and accumulation used by the Kronecker head."""
     from vmc_torch_gb300 import _lib
     g = torch.Generator().manual_seed(Ns)
@@ -89,7 +110,7 @@ def test_tensor_core_gram_matches_compensated_fp32(Ns, K):
     scale = T_ref.diagonal().abs().max().item()
     err = (T - T_ref).abs().max().item() / scale
     print("tensor-core Gram (%d x %d): max rel err %.2e" % (Ns, K, err))
-    assert err < 1e-5
+    assert err < 2e-6
     assert torch.equal(T, T.t())
     # head form: T += alpha (X X^T) o D
     D = torch.rand((Ns, Ns), generator=g, dtype=torch.float64).to(DEV)
@@ -98,7 +119,7 @@ def test_tensor_core_gram_matches_compensated_fp32(Ns, K):
     solver._tc_gram(X, T2, 0.5, D, 0.0, 1, DEV)
     ref2 = T_ref + 0.5 * (T_ref - 1e-3 * torch.eye(Ns, dtype=torch.float64, device=DEV)) * D
     err2 = (T2 - ref2).abs().max().item() / scale
-    assert err2 < 2e-5
+    assert err2 < 4e-6
 
 
 def test_minsr_tensor_gram_vs_cuda_gram_mixed():

@@ -64,8 +64,8 @@ SIGNATURES = {
     "vmc_sr_center": [P, I32, I64, I64, I64, P, I64, P, P],
     "vmc_sr_gram": [P, I32, I64, I64, I64, P, I64, F64, I32, P],
     "vmc_sr_cholesky": [P, I64, I64, P, P],
-    "vmc_split_bf16x3": [P, I64, I64, I64, P, I64, I64, P],
-    "vmc_sr_gram_tc": [P, I64, I64, I64, F64, P, I64, P, F64, I32, P, P],
+    "vmc_split_bf16x3": [P, I64, I64, I64, P, I64, I64, P, P],
+    "vmc_sr_gram_tc": [P, P, I64, I64, I64, F64, P, I64, P, F64, I32, P, P],
     "vmc_sr_cholesky_solve": [P, I64, I64, P, P],
     "vmc_sr_rhs": [P, I64, F64, P, P],
     "vmc_sr_update": [P, I32, I64, I64, I64, P, P, P],

@@ -4,16 +4,21 @@
 //
 // for an FP32 matrix X (Ns x K): the per-sample log-derivatives, centred and
 // scaled (the dense block of O), or the Kronecker factor G of the NNBF output
-// layer (with D = H H^T).  FP32 accuracy on BF16 tensor cores: every entry is
-// split as x = hi + mid + lo with hi = bf16(x), mid = bf16(x - hi),
-// lo = bf16(x - hi - mid) (24 bits of mantissa, the FP32 value to within
-// 2^-24), and the product x_i x_j is taken as the six terms
-//   hi hi + hi mid + mid hi + hi lo + lo hi + mid mid
-// (the three dropped terms are below 2^-24 relative).  The products are exact
-// in FP32.  The leading term hi hi accumulates in one TMEM accumulator and the
-// five small terms (2^-8 of it and below) in a second, so the FP32 rounding of
-// the large running sum happens once per K=16 step of a single product; both
-// are drained into the FP64 result every 2048 columns of K.
+// layer (with D = H H^T).  Fixed-point split (the Ozaki scheme's idea): each
+// row i gets a shared power-of-two exponent E_i (its largest |x| below
+// 2^E_i), and y = x 2^-E_i is written as three 7-bit integer digits,
+//   y = 2^-6 a0 + 2^-13 a1 + 2^-20 a2,  a_s in [-64, 64]
+// (to 2^-20 of the row's largest entry), each digit scaled by its power of two
+// exactly representable in BF16.  The product y_i y_j is taken as all nine
+// digit products (hi, mid, lo the three planes), so the result is exactly the
+// Gram matrix of the rounded rows and stays positive semidefinite.  The
+// leading term hi hi is an integer multiple of 2^-12 of magnitude <= 1, so its
+// FP32 running sum over a 2048-column chunk (<= 2^23 units) is exact: it
+// accumulates in its own TMEM accumulator with no rounding at all.  The eight
+// small terms (2^-7 of it and below) share a second accumulator, where FP32
+// rounding is ~2^-25 of 2^-7 of the result.
+// Both are drained into the FP64 result every 2048 columns of K, scaled by
+// 2^(E_i + E_j).
 //
 // Tile: 128 x 128 outputs per CTA, lower triangle of tiles only (the upper
 // triangle is written as the mirror image).  K atoms of 64 BF16 (128 bytes per
@@ -39,29 +44,48 @@ constexpr int CHUNK_ATOMS = 32;               // 2048 columns of K per FP32 accu
 constexpr int GR_THREADS = 192;
 constexpr int GR_SMEM = NSTAGE * STAGE + 1024 + 256;
 
-// x -> (hi, mid, lo) planes (plane p at P + p * plane), row-major with row
-// stride kp; rows >= `rows` and columns >= K are zero.
+// Row exponents: E[r] = ilogb(max_k |X[r][k]|) + 1 (0 for a zero row or a
+// padding row), one warp per row.
+__global__ void k_row_exp(const float* __restrict__ X, int64_t rows, int64_t rows_pad, int64_t K, int64_t ldx,
+                          int* __restrict__ E) {
+  const int64_t r = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (r >= rows_pad) return;
+  float m = 0.f;
+  if (r < rows)
+    for (int64_t c = lane; c < K; c += 32) m = fmaxf(m, fabsf(X[r * ldx + c]));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(VMC_FULL_MASK, m, o));
+  if (lane == 0) E[r] = (m > 0.f && m < INFINITY) ? ilogbf(m) + 1 : 0;
+}
+
+// x -> (hi, mid, lo) planes of the fixed-point digits of x 2^-E[r] (plane p at
+// P + p * plane), row-major with row stride kp; rows >= `rows` and columns >=
+// K are zero.  Every step below is exact in FP32: scaling by powers of two,
+// rounding to an integer, and the subtraction of that integer from a value
+// within 0.5 of it.
 __global__ void k_split3(const float* __restrict__ X, int64_t rows, int64_t rows_pad, int64_t K, int64_t ldx,
-                         int64_t kp, __nv_bfloat16* __restrict__ P) {
+                         int64_t kp, const int* __restrict__ E, __nv_bfloat16* __restrict__ P) {
   const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= rows_pad * kp) return;
   const int64_t r = idx / kp, c = idx - r * kp;
   const float x = (r < rows && c < K) ? X[r * ldx + c] : 0.f;
-  const __nv_bfloat16 h = __float2bfloat16_rn(x);
-  const float r1 = x - __bfloat162float(h);
-  const __nv_bfloat16 m = __float2bfloat16_rn(r1);
-  const float r2 = r1 - __bfloat162float(m);
-  const __nv_bfloat16 l = __float2bfloat16_rn(r2);
+  const float y = ldexpf(x, 6 - E[r]);       // 2^6 x 2^-E, |y| < 64
+  const float a0 = rintf(y);
+  const float r1 = (y - a0) * 128.f;         // |r1| <= 64
+  const float a1 = rintf(r1);
+  const float a2 = rintf((r1 - a1) * 128.f);
   const int64_t plane = rows_pad * kp;
-  P[idx] = h;
-  P[plane + idx] = m;
-  P[2 * plane + idx] = l;
+  P[idx] = __float2bfloat16_rn(ldexpf(a0, -6));
+  P[plane + idx] = __float2bfloat16_rn(ldexpf(a1, -13));
+  P[2 * plane + idx] = __float2bfloat16_rn(ldexpf(a2, -20));
 }
 
 struct GramArgs {
   double* T;
   int64_t ldt;
   const double* D;   // nullable, ld = ldt
+  const int* E;      // row exponents of the split
   double alpha, shift;
   int n;             // rows of X (order of T)
   int prow;          // rows per plane (n rounded up to the tile)
@@ -125,9 +149,9 @@ __global__ void __launch_bounds__(GR_THREADS, 1)
   } else if (warp == 1) {
     if (lane == 0) {  // ---- MMA issuer ----
       constexpr uint32_t idesc = tc::idesc_bf16_f32(GT, GT);
-      // (A plane, B plane) of the six products
-      constexpr int pa[6] = {0, 0, 1, 0, 2, 1};
-      constexpr int pb[6] = {0, 1, 0, 2, 0, 1};
+      // (A plane, B plane) of the nine products: the leading one, then the rest
+      constexpr int pa[9] = {0, 0, 1, 0, 2, 1, 1, 2, 2};
+      constexpr int pb[9] = {0, 1, 0, 2, 0, 1, 2, 1, 2};
       for (int c = 0; c < n_chunks && !*abort_flag; ++c) {
         const int buf = c & 1;
         if (c >= 2 && !tc::mbar_wait(&tempty[buf], ((c >> 1) - 1) & 1)) {
@@ -145,7 +169,7 @@ __global__ void __launch_bounds__(GR_THREADS, 1)
           tc::fence_after_sync();
           const uint8_t* st = sm + s * STAGE;
 #pragma unroll
-          for (int q = 0; q < 6; ++q) {
+          for (int q = 0; q < 9; ++q) {
 #pragma unroll
             for (int kk = 0; kk < 4; ++kk) {
               const uint64_t ad = tc::sdesc_sw128(tc::smem_u32(st + pa[q] * PLANE) + kk * 32);
@@ -185,7 +209,7 @@ __global__ void __launch_bounds__(GR_THREADS, 1)
           const int64_t gj = (int64_t)bj * GT + cc * 32 + q;
           if (gj >= ga.n || (bi == bj && gj > gi)) continue;
           double* t = ga.T + gi * ga.ldt + gj;
-          double add = ga.alpha * ((double)v[q] + (double)w[q]);
+          double add = ga.alpha * ldexp((double)v[q] + (double)w[q], ga.E[gi] + ga.E[gj]);
           if (ga.D) add *= ga.D[gi * ga.ldt + gj];
           double val = first ? add : *t + add;
           if (last && gj == gi) val += ga.shift;
@@ -236,22 +260,25 @@ extern "C" {
 // planes: 3 * rows_pad * kp bf16 workspace, rows_pad = rows rounded up to 128,
 // kp = K rounded up to 64.  Rows beyond `rows` are zeroed.
 int vmc_split_bf16x3(const float* X, int64_t rows, int64_t K, int64_t ldx, void* planes, int64_t rows_pad,
-                     int64_t kp, void* stream) {
+                     int64_t kp, int* row_exp, void* stream) {
   if (rows < 0 || K < 0 || ldx < K || rows_pad < rows || rows_pad % GT != 0 || kp < K || kp % KA != 0 ||
-      (rows > 0 && (!X || !planes)))
+      (rows > 0 && (!X || !planes)) || (rows_pad > 0 && !row_exp))
     return VMC_ERR_ARGS;
   if (rows_pad == 0) return VMC_OK;
+  k_row_exp<<<(unsigned)((rows_pad + 7) / 8), 256, 0, (cudaStream_t)stream>>>(X, rows, rows_pad, K, ldx, row_exp);
+  VMC_CUDA_CHECK_LAUNCH();
   const int64_t n = rows_pad * kp;
-  k_split3<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(X, rows, rows_pad, K, ldx, kp,
+  k_split3<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(X, rows, rows_pad, K, ldx, kp, row_exp,
                                                                           (__nv_bfloat16*)planes);
   VMC_CUDA_CHECK_LAUNCH();
   return VMC_OK;
 }
 
-int vmc_sr_gram_tc(const void* planes, int64_t ns, int64_t rows_pad, int64_t kp, double alpha, double* T,
-                   int64_t ldt, const double* D, double diag_shift, int accumulate, int* d_err, void* stream) {
+int vmc_sr_gram_tc(const void* planes, const int* row_exp, int64_t ns, int64_t rows_pad, int64_t kp, double alpha,
+                   double* T, int64_t ldt, const double* D, double diag_shift, int accumulate, int* d_err,
+                   void* stream) {
   if (ns <= 0 || rows_pad < ns || rows_pad % GT != 0 || kp <= 0 || kp % KA != 0 || ldt < ns || !planes || !T ||
-      !d_err || ns > (1 << 30))
+      !d_err || !row_exp || ns > (1 << 30))
     return VMC_ERR_ARGS;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDev) return VMC_ERR_CUDA;
@@ -263,7 +290,7 @@ int vmc_sr_gram_tc(const void* planes, int64_t ns, int64_t rows_pad, int64_t kp,
   CUtensorMap tm;
   if (!tmap_planes(&tm, planes, (uint64_t)(3 * rows_pad), (uint64_t)kp)) return VMC_ERR_UNSUPPORTED;
   const int nt = (int)(rows_pad / GT);
-  GramArgs ga{T, ldt, D, alpha, diag_shift, (int)ns, (int)rows_pad, (int)(kp / KA), accumulate};
+  GramArgs ga{T, ldt, D, row_exp, alpha, diag_shift, (int)ns, (int)rows_pad, (int)(kp / KA), accumulate};
   const int n_tiles = nt * (nt + 1) / 2;
   k_gram_bf16x3<<<(unsigned)n_tiles, GR_THREADS, GR_SMEM, (cudaStream_t)stream>>>(tm, ga, d_err);
   VMC_CUDA_CHECK_LAUNCH();

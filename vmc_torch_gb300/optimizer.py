@@ -134,12 +134,12 @@ class MinSRGB300(PreconditionerGB300):
     def __init__(self, record_stages=False, gram="cuda"):
         """gram: "cuda" (default) forms the Gram blocks of FP32 O on the CUDA
         cores with compensated (double-float) accumulation, FP64-level.
-        "tensor" forms them on the tensor cores (vmc_sr_gram_tc: BF16
-        three-way split, six products, FP32 partial sums drained into FP64
-        every 2048 columns): ~6x faster, but its entries carry ~5e-6 of the
-        largest diagonal entry in rounding, so use it only where the diagonal
-        shift is well above that (at 16384 samples and shift 1e-4 the rounding
-        makes T indefinite).  FP64 O always uses FP64 arithmetic."""
+        "tensor" forms them on the tensor cores (vmc_sr_gram_tc: each row split
+        into three 7-bit fixed-point digits under a shared power-of-two
+        exponent, all nine digit products, the leading one summed exactly in
+        FP32, drained into FP64 every 2048 columns): the Gram matrix of the
+        rows rounded to 2^-20 of their largest entry, positive semidefinite
+        up to ~2^-32 rounding.  FP64 O always uses FP64 arithmetic."""
         if gram not in ("tensor", "cuda"):
             raise ValueError("gram must be 'tensor' or 'cuda'")
         self.record_stages = record_stages
@@ -152,10 +152,11 @@ class MinSRGB300(PreconditionerGB300):
         Ns, K = X.shape
         rp, kp = -(-Ns // 128) * 128, -(-K // 64) * 64
         planes = torch.empty(3 * rp * kp, dtype=torch.bfloat16, device=dev)
-        _lib.call("vmc_split_bf16x3", _lib.ptr(X), Ns, K, X.stride(0), _lib.ptr(planes), rp, kp, s)
+        rexp = torch.empty(rp, dtype=torch.int32, device=dev)
+        _lib.call("vmc_split_bf16x3", _lib.ptr(X), Ns, K, X.stride(0), _lib.ptr(planes), rp, kp, _lib.ptr(rexp), s)
         err = torch.zeros(1, dtype=torch.int32, device=dev)
-        _lib.call("vmc_sr_gram_tc", _lib.ptr(planes), Ns, rp, kp, float(alpha), _lib.ptr(T), T.stride(0),
-                  _lib.ptr(D), float(shift), int(accumulate), _lib.ptr(err), s)
+        _lib.call("vmc_sr_gram_tc", _lib.ptr(planes), _lib.ptr(rexp), Ns, rp, kp, float(alpha), _lib.ptr(T),
+                  T.stride(0), _lib.ptr(D), float(shift), int(accumulate), _lib.ptr(err), s)
         self._tc_err = err
         del planes
 
