@@ -504,9 +504,10 @@ def ess_block(dev, n_walkers, samples=192, discard=32, moves=14, sr_steps=20, pr
 def sr_block(model, H, fxs, dev, fp32_peak_tflops, diag_shift=1e-4):
     """Configs 2-3's SR path at the headline size: the hand-written adjoint O
     (dense block + Kronecker factors of the out_w block) for every walker, the
-    local energies, then minSR (centring, dense Gram on FP32 CUDA cores with
-    compensated accumulation, the Kronecker-corrected head block, FP64
-    Cholesky, solves, update).  Device time per stage (CUDA events on the
+    local energies, then minSR (centring, dense Gram on the tensor cores with
+    the fixed-point digit split, the Kronecker-corrected head block, FP64
+    Cholesky, solves, update); the same solve with the CUDA-core Gram is
+    timed beside it with the difference of the two directions.  Device time per stage (CUDA events on the
     current stream) and the algorithmic FLOP of each: dense Gram
     2 Ns^2 Np_dense, head 2 Ns^2 (2N nf + 256) (+ the mean 2 Ns 2N nf 256),
     Cholesky Ns^3 / 3."""
@@ -555,12 +556,16 @@ def sr_block(model, H, fxs, dev, fp32_peak_tflops, diag_shift=1e-4):
             d["flop"] = fl[k]
         stages[k] = d
     if "gram_dense" in stages:
-        stages["gram_dense"]["frac_of_fp32_nominal"] = stages["gram_dense"]["tflops"] / fp32_peak_tflops
+        # nine BF16 products per counted multiply-add, on the lower triangle of 128 x 128 tiles only
+        nt = -(-Ns // 128)
+        ex = 9 * stages["gram_dense"]["tflops"] * (nt + 1) / (2.0 * nt)
+        stages["gram_dense"]["tensor_tflops_executed"] = ex
+        stages["gram_dense"]["frac_of_bf16_measured"] = ex / peaks()["bf16_tflops"]
     if "cholesky" in stages:
         stages["cholesky"]["frac_of_fp64_nominal"] = stages["cholesky"]["tflops"] / 1.25
     o_bytes = Ns * (Nd + Ng + Nh) * F.dense.element_size()
-    # the same solve with the Gram blocks on the tensor cores (fixed-point digit split, exact leading sums)
-    tsolver = vg.MinSRGB300(record_stages=True, gram="tensor")
+    # the same solve with the Gram blocks on the CUDA cores (compensated accumulation: the exact Gram of the FP32 rows)
+    tsolver = vg.MinSRGB300(record_stages=True, gram="cuda")
     tsolver.solve(local_o=F, local_energies=E, energy_mean=float(E.mean()), total_samples=Ns,
                   n_params=model.n_params, diag_shift=diag_shift, device=dev, run_sr=True)   # warm-up
     (dpt, _, tinfo), tsr_ms = timed(lambda: tsolver.solve(local_o=F, local_energies=E, energy_mean=float(E.mean()),
@@ -572,13 +577,13 @@ def sr_block(model, H, fxs, dev, fp32_peak_tflops, diag_shift=1e-4):
         if k in fl:
             d["tflops"] = fl[k] / (ms / 1e3) / 1e12
         tstages[k] = d
-    tensor = {"minsr_ms": tsr_ms, "minsr_stages": tstages, "info": tinfo,
-              "dp_rel_diff_vs_cuda_gram": float((dpt - dp).norm().item() / dp.norm().item())}
+    cuda_gram = {"minsr_ms": tsr_ms, "minsr_stages": tstages, "info": tinfo,
+                 "dp_rel_diff_vs_tensor_gram": float((dpt - dp).norm().item() / dp.norm().item())}
     return {"workload": "8x8 NNBF, %d walkers: per-sample O (FP32, dense %d + Kronecker %d x %d), E_loc, minSR "
                         "over %d parameters (diag shift %g)" % (Ns, Nd, Ng, Nh, model.n_params, diag_shift),
             "logpsi_grad_ms": grad_ms, "first_full_size_call": first, "O_bytes_written": o_bytes,
             "O_write_gbs": o_bytes / (grad_ms / 1e3) / 1e9, "local_energy_ms": eloc_ms, "minsr_ms": sr_ms,
-            "minsr_stages": stages, "info": info, "dp_norm": float(dp.norm().item()), "tensor_gram": tensor,
+            "minsr_stages": stages, "info": info, "dp_norm": float(dp.norm().item()), "cuda_gram": cuda_gram,
             "peaks": "FP32 nominal %.1f TFLOP/s (152 SM x 128 lanes x 2 x max SM clock), FP64 nominal 1.25 TFLOP/s"
                      % fp32_peak_tflops}
 

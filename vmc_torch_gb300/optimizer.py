@@ -131,15 +131,16 @@ class MinSRGB300(PreconditionerGB300):
     (centring, Gram blocks, Cholesky, triangular solves, update) in
     ``last_stages`` (milliseconds, CUDA events on the current stream)."""
 
-    def __init__(self, record_stages=False, gram="cuda"):
-        """gram: "cuda" (default) forms the Gram blocks of FP32 O on the CUDA
-        cores with compensated (double-float) accumulation, FP64-level.
-        "tensor" forms them on the tensor cores (vmc_sr_gram_tc: each row split
+    def __init__(self, record_stages=False, gram="tensor"):
+        """gram: "tensor" (default) forms the Gram blocks of FP32 O on the
+        tensor cores (vmc_sr_gram_tc: each row split
         into three 7-bit fixed-point digits under a shared power-of-two
         exponent, all nine digit products, the leading one summed exactly in
         FP32, drained into FP64 every 2048 columns): the Gram matrix of the
         rows rounded to 2^-20 of their largest entry, positive semidefinite
-        up to ~2^-32 rounding.  FP64 O always uses FP64 arithmetic."""
+        up to ~2^-32 rounding.  "cuda" forms them on the CUDA cores with
+        compensated (double-float) accumulation: the exact Gram of the FP32
+        rows, ~10x slower.  FP64 O always uses FP64 arithmetic."""
         if gram not in ("tensor", "cuda"):
             raise ValueError("gram must be 'tensor' or 'cuda'")
         self.record_stages = record_stages
