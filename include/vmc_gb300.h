@@ -194,8 +194,10 @@ int vmc_prop_sample(const int32_t* edges, int n_edges, int n_sites, const float*
 /* log q(x'->x) from the logits at the proposed configurations. */
 int vmc_prop_reverse(const int32_t* edges, int n_edges, int n_sites, const float* logits_p, const uint64_t* prop_occ,
                      int64_t B, void* rec, void* stream);
-/* MH accept of learned proposals for the mixed NNBF model: psi(x') evaluated
- * from scratch (z0p workspace), accept with min(1, |psi'/psi|^2 q(x'->x)/q(x->x')).
+/* MH accept of learned proposals for the mixed NNBF model: psi(x') evaluated with
+ * its first layer z0p = z0 + the W0 columns of the orbitals the proposal changes
+ * (z0: the walkers' first layer, as left by vmc_nnbf_eval; z0p workspace, copied
+ * into z0 on acceptance), accept with min(1, |psi'/psi|^2 q(x'->x)/q(x->x')).
  * Optional: lg_x (B, 256) proposal logits at x, overwritten with lg_p's row when a
  * walker moves (so the next move needs only the logits at its new proposal);
  * kstats[8] device counters of proposals / acceptances by k. */

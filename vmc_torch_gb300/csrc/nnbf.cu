@@ -192,6 +192,47 @@ __global__ void k_prep_fresh(int64_t R, int N, int nf, const uint64_t* __restric
   H1Store<T>::store(H1, w, lane, h);
 }
 
+// First layer of proposals that differ from the current configurations in a
+// few orbitals (a learned move of k <= 4 hops changes at most 8): z0p = z0 +
+// the W0 columns of the orbitals the proposal fills - those it empties, then
+// GELU -> BF16 row.  z0 is the current configuration's cached first layer
+// (rebuilt from scratch whenever the walkers are bound or refreshed).
+template <typename T>
+__global__ void k_prep_delta(int64_t R, int N, int nf, const uint64_t* __restrict__ occ,
+                             const uint64_t* __restrict__ prop_occ, const T* __restrict__ z0,
+                             const T* __restrict__ w0t, T* __restrict__ z0p, void* __restrict__ H1,
+                             int* __restrict__ err) {
+  const int lane = threadIdx.x & 31;
+  const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (w >= R) return;
+  const uint64_t keep = bits_below(N);
+  const uint64_t pu_raw = prop_occ[2 * w], pd_raw = prop_occ[2 * w + 1];
+  const uint64_t pu = pu_raw & keep, pd = pd_raw & keep;
+  if (lane == 0 && err && (((pu_raw | pd_raw) & ~keep) != 0ull || __popcll(pu) + __popcll(pd) != nf))
+    atomicExch(err, VMC_ERR_ARGS);
+  const uint64_t cu = occ[2 * w] & keep, cd = occ[2 * w + 1] & keep;
+  T h[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) h[q] = z0[w * HID + lane * 8 + q];
+  for (int sp = 0; sp < 2; ++sp) {
+    const uint64_t pm = sp ? pd : pu;
+    uint64_t m = pm ^ (sp ? cd : cu);
+    while (m) {
+      const int site = __ffsll((long long)m) - 1;
+      m &= m - 1;
+      const T sg = ((pm >> site) & 1ull) ? T(1) : T(-1);
+      const int o = sp * N + site;
+#pragma unroll
+      for (int q = 0; q < 8; ++q) h[q] += sg * w0t[o * HID + lane * 8 + q];
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < 8; ++q) z0p[w * HID + lane * 8 + q] = h[q];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) h[q] = gelu_t<T>(h[q]);
+  H1Store<T>::store(H1, w, lane, h);
+}
+
 // Local-energy prep: pair p = (walker, hop term) -> connected configuration
 // occupation, coefficient, z0 + W0 column difference, h1.
 template <typename T>
@@ -2109,7 +2150,9 @@ extern "C" int vmc_nnbf_hidden_layer(const void* H1, int64_t R, const void* W1, 
 
 // Metropolis-Hastings step with a learned proposal (mixed precision): the
 // proposals (prop_occ, rec4 from vmc_prop_sample / vmc_prop_reverse) are
-// evaluated from scratch and accepted with min(1, |psi'/psi|^2 q(x'->x)/q(x->x')).
+// evaluated (first layer updated from the walkers' cached z0 over the changed
+// orbitals, the rest in full) and accepted with
+// min(1, |psi'/psi|^2 q(x'->x)/q(x->x')).
 // Workspace: z0p (B, 256) f32, H1/H2/A for B rows.
 extern "C" int vmc_nnbf_mh_step(const void* const* net_ptrs, int n_sites, int nf, int hidden, double bf_scale,
                                 uint64_t* occ, int64_t B, const uint64_t* prop_occ, const void* rec4, void* z0,
@@ -2127,7 +2170,8 @@ extern "C" int vmc_nnbf_mh_step(const void* const* net_ptrs, int n_sites, int nf
              (const float*)net_ptrs[3], (const __nv_bfloat16*)net_ptrs[4], (const float*)net_ptrs[5],
              (const float*)net_ptrs[6]};
   const unsigned gw = (unsigned)((B * 32 + 255) / 256);
-  k_prep_fresh<float><<<gw, 256, 0, st>>>(B, n_sites, nf, prop_occ, n32.w0t, n32.b0, (float*)z0p, H1, d_err);
+  k_prep_delta<float><<<gw, 256, 0, st>>>(B, n_sites, nf, occ, prop_occ, (const float*)z0, n32.w0t, (float*)z0p, H1,
+                                          d_err);
   VMC_CUDA_CHECK_LAUNCH();
   LdArgs la{};
   la.rec4 = (const PropRec4*)rec4;
