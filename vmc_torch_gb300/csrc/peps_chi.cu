@@ -479,7 +479,7 @@ struct ChiTruncSmem {
 // item's two warps have ranked their eigenvalues together projects its block
 // of the state onto the kept eigenvectors.  The state stays in global memory
 // (L2-resident).
-template <typename T, int D>
+template <typename T, int D, bool ONE_SIDED>
 __global__ void __launch_bounds__(32 * 2 * CHI_TRUNC_ITEMS)
     k_chi_trunc(ChiSched sc, int k, int n_rows, const uint64_t* __restrict__ cfg,
                 const int32_t* __restrict__ cfg_idx, const uint8_t* __restrict__ sides, int64_t n_items,
@@ -517,8 +517,8 @@ __global__ void __launch_bounds__(32 * 2 * CHI_TRUNC_ITEMS)
   auto at = [&](uint32_t p, uint32_t q) -> int64_t {
     return left ? (int64_t)p * nR + q : (int64_t)q * nR + p;
   };
-  if (nq <= 32) {
-    // the block fits a warp's registers (the middle cut of a 6-wide lattice): one-sided Jacobi on its rows
+  if constexpr (ONE_SIDED) {
+    // the block fits a warp's registers (nq <= 32: the middle cut of a 6-wide lattice): one-sided Jacobi on its rows
     T u[32];
 #pragma unroll
     for (int j = 0; j < 32; ++j)
@@ -556,9 +556,7 @@ __global__ void __launch_bounds__(32 * 2 * CHI_TRUNC_ITEMS)
   __syncwarp();
   // projection of the block onto the kept eigenvectors, one big-side column at a time
   if (on) {
-    T vi[32];
-#pragma unroll
-    for (int j = 0; j < 32; ++j) vi[j] = V[ln * 33 + j];
+    const T* vi = V + ln * 33;   // eigenvector ln, read from shared memory (keeps registers for the Jacobi)
     const bool kp = keep[b * 32 + ln] != 0;
     for (int iq = 0; iq < nq; ++iq) {
       const uint32_t q = block_member<D>(qcls, iq);
@@ -1110,7 +1108,10 @@ int build_sides_d(const void* tens, const ChiSched& sc, const uint64_t* cfg, con
   if (cudaFuncSetAttribute(k_chi_absorb<T, D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return VMC_ERR_CUDA;
   const size_t tsm = ChiTruncSmem<T>::bytes();
-  if (cudaFuncSetAttribute(k_chi_trunc<T, D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm) != cudaSuccess)
+  if (cudaFuncSetAttribute(k_chi_trunc<T, D, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm) !=
+          cudaSuccess ||
+      cudaFuncSetAttribute(k_chi_trunc<T, D, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm) !=
+          cudaSuccess)
     return VMC_ERR_CUDA;
   int a = 0;
   while (a < sc.rows) {
@@ -1121,8 +1122,16 @@ int build_sides_d(const void* tens, const ChiSched& sc, const uint64_t* cfg, con
     VMC_CUDA_CHECK_LAUNCH();
     for (int k = sc.Ly - 1; k >= 1; --k)
       if ((sc.cuts[a1 - 1] >> k) & 1u) {
-        k_chi_trunc<T, D><<<(unsigned)((n_items + CHI_TRUNC_ITEMS - 1) / CHI_TRUNC_ITEMS), 64 * CHI_TRUNC_ITEMS, tsm,
-                            st>>>(sc, k, a1, cfg, cfg_idx, sides, n_items, count, state, ex);
+        int nL = 1;
+        for (int i = 0; i < k; ++i) nL *= D;
+        const int n = nL <= sc.NS / nL ? nL : sc.NS / nL;
+        const unsigned grid = (unsigned)((n_items + CHI_TRUNC_ITEMS - 1) / CHI_TRUNC_ITEMS);
+        if ((sc.NS / n) / 2 <= 32)
+          k_chi_trunc<T, D, true><<<grid, 64 * CHI_TRUNC_ITEMS, tsm, st>>>(sc, k, a1, cfg, cfg_idx, sides, n_items,
+                                                                            count, state, ex);
+        else
+          k_chi_trunc<T, D, false><<<grid, 64 * CHI_TRUNC_ITEMS, tsm, st>>>(sc, k, a1, cfg, cfg_idx, sides, n_items,
+                                                                             count, state, ex);
         VMC_CUDA_CHECK_LAUNCH();
       }
     a = a1;
