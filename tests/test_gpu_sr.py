@@ -89,7 +89,7 @@ def test_tensor_core_gram_is_exact_on_digit_representable_rows():
     assert torch.equal(T, ref)
 
 
-@pytest.mark.parametrize("Ns,K", [(700, 3000), (256, 115200 // 16)])
+@pytest.mark.parametrize("Ns,K", [(700, 3000), (256, 115200 // 16), (4096, 16384)])
 def test_tensor_core_gram_matches_compensated_fp32(Ns, K):
     """vmc_sr_gram_tc (fixed-point 7-bit digits under a per-row exponent, nine
     products on tcgen05, the leading one summed exactly, drained into FP64)
