@@ -69,3 +69,22 @@ def test_chi_schedule_truncates_one_cut_at_6x6_chi16():
     assert peps.chi_schedule(6, 6, 4, 16) == [[], [], [3]]
     assert peps.chi_schedule(6, 6, 4, 64) == [[], [], []]
     assert peps.chi_schedule(6, 6, 4, 8) == [[], [4, 3, 2], [4, 3, 2]]
+
+
+def test_chi_gradient_oracle_matches_finite_differences():
+    """The oracle's O through the chi truncation (torch autograd through
+    torch.linalg.svd, as the reference differentiates its contraction)
+    against central differences (h = 1e-6) of the FP64 truncated amplitude."""
+    T = peps.init_tensors(4, 4, 4, seed=4)
+    x = lattice.random_initial_configs(1, 16, 4, 4, seed=3)[0]
+    g = peps.logamp_grad_chi(T, x, 8)
+    nz = np.argwhere(np.abs(g) > 1e-8)
+    rng = np.random.default_rng(0)
+    for idx in nz[rng.choice(len(nz), 8, replace=False)]:
+        idx = tuple(idx)
+        h = 1e-6 * max(1.0, abs(T[idx]))
+        Tp, Tm = T.copy(), T.copy()
+        Tp[idx] += h
+        Tm[idx] -= h
+        fd = (np.log(abs(peps.amp_state_chi(Tp, x, 8))) - np.log(abs(peps.amp_state_chi(Tm, x, 8)))) / (2 * h)
+        assert abs(fd - g[idx]) <= 1e-5 * max(abs(fd), 1e-3)
