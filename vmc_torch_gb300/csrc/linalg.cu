@@ -176,26 +176,55 @@ __global__ void k_trsm_panel(double* __restrict__ C, int64_t ldc, int64_t n, int
   for (int k = 0; k < nb; ++k) a[k] = x[k];
 }
 
-// Single-block triangular solves with the lower factor L (ld ldc):
-// trans = 0: L y = b;  trans = 1: L^T x = b.  In place on b.
-__global__ void k_trsv(const double* __restrict__ L, int64_t ldc, int64_t n, double* __restrict__ b, int trans) {
+// Blocked triangular solves (panels of TRSV_NB rows): the diagonal block is
+// solved by one CTA (thread t owns row t of the block), then every remaining
+// row is updated by a coalesced dot with the panel's solved values.
+constexpr int TRSV_NB = 64;
+
+// trans = 0: solve L[k0:k0+nb, k0:k0+nb] y = b[k0:k0+nb] in place (forward);
+// trans = 1: solve L[k0:k0+nb, k0:k0+nb]^T x = b[k0:k0+nb] in place (backward).
+__global__ void k_trsv_diag(const double* __restrict__ L, int64_t ldc, int64_t k0, int nb, double* __restrict__ b,
+                            int trans) {
+  __shared__ double xs[TRSV_NB];
+  const int t = threadIdx.x;
+  double bt = t < nb ? b[k0 + t] : 0.0;
   if (!trans) {
-    for (int64_t j = 0; j < n; ++j) {
+    for (int j = 0; j < nb; ++j) {
+      if (t == j) xs[j] = bt / L[(k0 + j) * ldc + k0 + j];
       __syncthreads();
-      double xj = b[j] / L[j * ldc + j];
-      __syncthreads();
-      if (threadIdx.x == 0) b[j] = xj;
-      for (int64_t i = j + 1 + threadIdx.x; i < n; i += blockDim.x) b[i] -= L[i * ldc + j] * xj;
+      if (t > j && t < nb) bt -= L[(k0 + t) * ldc + k0 + j] * xs[j];
     }
   } else {
-    for (int64_t j = n - 1; j >= 0; --j) {
+    for (int j = nb - 1; j >= 0; --j) {
+      if (t == j) xs[j] = bt / L[(k0 + j) * ldc + k0 + j];
       __syncthreads();
-      double xj = b[j] / L[j * ldc + j];
-      __syncthreads();
-      if (threadIdx.x == 0) b[j] = xj;
-      for (int64_t i = threadIdx.x; i < j; i += blockDim.x) b[i] -= L[j * ldc + i] * xj;
+      if (t < j) bt -= L[(k0 + j) * ldc + k0 + t] * xs[j];
     }
   }
+  if (t < nb) b[k0 + t] = xs[t];
+}
+
+// forward update: b[i] -= sum_{j < nb} L[i][k0 + j] b[k0 + j] for rows i >= k0 + nb, a warp per row
+__global__ void k_trsv_upd_fwd(const double* __restrict__ L, int64_t ldc, int64_t n, int64_t k0, int nb,
+                               double* __restrict__ b) {
+  const int64_t i = k0 + nb + (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (i >= n) return;
+  double acc = 0.0;
+  for (int j = lane; j < nb; j += 32) acc += L[i * ldc + k0 + j] * b[k0 + j];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (lane == 0) b[i] -= acc;
+}
+
+// backward update: b[j] -= sum_{i < nb} L[k0 + i][j] b[k0 + i] for columns j < k0, a thread per column
+__global__ void k_trsv_upd_bwd(const double* __restrict__ L, int64_t ldc, int64_t k0, int nb,
+                               double* __restrict__ b) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= k0) return;
+  double acc = 0.0;
+  for (int i = 0; i < nb; ++i) acc += L[(k0 + i) * ldc + j] * b[k0 + i];
+  b[j] -= acc;
 }
 
 // dp[p] = sum_i Oc[i][p] * x[i]
@@ -287,8 +316,19 @@ int vmc_sr_cholesky(double* T, int64_t n, int64_t ldt, int* d_info, void* stream
 // Solve L L^T x = b in place on b (L from vmc_sr_cholesky).
 int vmc_sr_cholesky_solve(const double* L, int64_t n, int64_t ldt, double* b, void* stream) {
   if (n <= 0 || ldt < n || !L || !b) return VMC_ERR_ARGS;
-  k_trsv<<<1, 1024, 0, (cudaStream_t)stream>>>(L, ldt, n, b, 0);
-  k_trsv<<<1, 1024, 0, (cudaStream_t)stream>>>(L, ldt, n, b, 1);
+  cudaStream_t st = (cudaStream_t)stream;
+  for (int64_t k0 = 0; k0 < n; k0 += TRSV_NB) {   // L y = b
+    const int nb = (int)((n - k0) < TRSV_NB ? (n - k0) : TRSV_NB);
+    k_trsv_diag<<<1, TRSV_NB, 0, st>>>(L, ldt, k0, nb, b, 0);
+    const int64_t rest = n - k0 - nb;
+    if (rest > 0) k_trsv_upd_fwd<<<(unsigned)((rest + 7) / 8), 256, 0, st>>>(L, ldt, n, k0, nb, b);
+  }
+  const int64_t last = ((n - 1) / TRSV_NB) * TRSV_NB;
+  for (int64_t k0 = last; k0 >= 0; k0 -= TRSV_NB) {   // L^T x = y
+    const int nb = (int)((n - k0) < TRSV_NB ? (n - k0) : TRSV_NB);
+    k_trsv_diag<<<1, TRSV_NB, 0, st>>>(L, ldt, k0, nb, b, 1);
+    if (k0 > 0) k_trsv_upd_bwd<<<(unsigned)((k0 + 255) / 256), 256, 0, st>>>(L, ldt, k0, nb, b);
+  }
   VMC_CUDA_CHECK_LAUNCH();
   return VMC_OK;
 }
