@@ -127,6 +127,73 @@ __global__ void k_syrk(const TI* __restrict__ A, int64_t lda, int64_t n, int64_t
     }
 }
 
+// The Cholesky's trailing update C -= A A^T for FP64 A in double-float
+// arithmetic on the FP32 pipes (GB300's FP64 rate is 1/64 of FP32): each
+// operand is split into FP32 x = hi + lo (to 2^-48), the leading product
+// hi*hi is captured exactly (p and its FMA error term), p is summed with
+// Knuth's TwoSum into a (s, c) pair and the small terms (the error term,
+// hi*lo + lo*hi) into a third FP32 accumulator; lo*lo (2^-48) is dropped.
+// ~12 FP32 instructions per multiply-add, relative accuracy ~2^-45 over the
+// tile, far below the Gram matrix's own input rounding.  Same tiling and
+// lower-triangle semantics as k_syrk.
+__global__ void k_syrk_df(const double* __restrict__ A, int64_t lda, int64_t n, int64_t K, double* __restrict__ C,
+                          int64_t ldc, int64_t off, double sgn) {
+  const int bi = blockIdx.y, bj = blockIdx.x;
+  if (bj > bi) return;
+  __shared__ float Ah[TK][TB + 1], Al[TK][TB + 1], Bh[TK][TB + 1], Bl[TK][TB + 1];
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  const int64_t i0 = off + (int64_t)bi * TB, j0 = off + (int64_t)bj * TB;
+  float hs[4][4], hc[4][4], sm[4][4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+#pragma unroll
+    for (int r = 0; r < 4; ++r) { hs[q][r] = 0.f; hc[q][r] = 0.f; sm[q][r] = 0.f; }
+  for (int64_t k0 = 0; k0 < K; k0 += TK) {
+    for (int idx = threadIdx.x; idx < TB * TK; idx += 256) {
+      const int r = idx / TK, kk = idx - r * TK;
+      const int64_t gk = k0 + kk, gi = i0 + r, gj = j0 + r;
+      const double a = (gi < off + n && gk < K) ? A[gi * lda + gk] : 0.0;
+      const double b = (gj < off + n && gk < K) ? A[gj * lda + gk] : 0.0;
+      const float ah = (float)a, bh = (float)b;
+      Ah[kk][r] = ah;
+      Al[kk][r] = (float)(a - (double)ah);
+      Bh[kk][r] = bh;
+      Bl[kk][r] = (float)(b - (double)bh);
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int kk = 0; kk < TK; ++kk) {
+      float ah[4], al[4], bh[4], bl[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        ah[q] = Ah[kk][ty * 4 + q]; al[q] = Al[kk][ty * 4 + q];
+        bh[q] = Bh[kk][tx * 4 + q]; bl[q] = Bl[kk][tx * 4 + q];
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+          const float p = ah[q] * bh[r];
+          const float e = fmaf(ah[q], bh[r], -p);
+          sm[q][r] += e + fmaf(ah[q], bl[r], al[q] * bh[r]);
+          const float s2 = hs[q][r] + p;
+          const float bb = s2 - hs[q][r];
+          hc[q][r] += (hs[q][r] - (s2 - bb)) + (p - bb);
+          hs[q][r] = s2;
+        }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int64_t gi = i0 + ty * 4 + q, gj = j0 + tx * 4 + r;
+      if (gi < off + n && gj < off + n && gj <= gi)
+        C[gi * ldc + gj] += sgn * ((double)hs[q][r] + (double)hc[q][r] + (double)sm[q][r]);
+    }
+}
+
 // Unblocked Cholesky of one diagonal tile (lower), in place; flags non-positive pivots.
 __global__ void k_potrf_tile(double* __restrict__ C, int64_t ldc, int64_t k0, int64_t nb, int* __restrict__ info) {
   __shared__ double a[TB][TB + 1];
@@ -305,8 +372,8 @@ int vmc_sr_cholesky(double* T, int64_t n, int64_t ldt, int* d_info, void* stream
       k_trsm_panel<<<(unsigned)((rest + 63) / 64), 64, 0, s>>>(T, ldt, n, k0, nb);
       int64_t nt = (rest + TB - 1) / TB;
       dim3 grid((unsigned)nt, (unsigned)nt);
-      // trailing update of the lower triangle: A22 -= L21 L21^T
-      k_syrk<double, double><<<grid, 256, 0, s>>>(T + k0, ldt, rest, nb, T, ldt, k0 + nb, -1.0, 0.0, 0);
+      // trailing update of the lower triangle: A22 -= L21 L21^T (double-float on the FP32 pipes)
+      k_syrk_df<<<grid, 256, 0, s>>>(T + k0, ldt, rest, nb, T, ldt, k0 + nb, -1.0);
     }
   }
   VMC_CUDA_CHECK_LAUNCH();
