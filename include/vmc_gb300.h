@@ -275,6 +275,11 @@ int vmc_sr_center(const void* O, int dtype, int64_t Ns, int64_t Np, int64_t ldo,
                   void* stream);
 int vmc_sr_gram(const void* Oc, int dtype, int64_t Ns, int64_t Np, int64_t ldc, double* T, int64_t ldt,
                 double diag_shift, int accumulate, void* stream);
+/* vmc_sr_cholesky: T = L L^T in place (lower), blocked right-looking with 64-column
+ *   panels; tile factorisations and panel solves in FP64, trailing updates in
+ *   double-float arithmetic on the FP32 pipes (~2^-46 relative per product sum).
+ *   *d_info is set to 1 when a pivot is not positive or not finite (the caller
+ *   zeroes it first); the factor is then not usable. */
 int vmc_sr_cholesky(double* T, int64_t n, int64_t ldt, int* d_info, void* stream);
 /* Tensor-core Gram for FP32 inputs (no reference counterpart as an operator:
  * the reference forms lpg_scaled @ lpg_scaled.T in FP64, vmc_torch/GPU/optimizer.py:551-553).

@@ -360,7 +360,8 @@ int vmc_sr_gram(const void* Oc, int dtype, int64_t Ns, int64_t Np, int64_t ldc, 
   return VMC_OK;
 }
 
-// In-place lower Cholesky of T (FP64).  d_info set to 1 on a non-positive pivot.
+// In-place lower Cholesky of T: FP64 tiles and panels, double-float trailing
+// updates.  d_info set to 1 on a non-positive pivot.
 int vmc_sr_cholesky(double* T, int64_t n, int64_t ldt, int* d_info, void* stream) {
   if (n <= 0 || ldt < n || !T || !d_info) return VMC_ERR_ARGS;
   cudaStream_t s = (cudaStream_t)stream;
