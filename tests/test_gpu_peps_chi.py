@@ -10,7 +10,7 @@ Tolerances: FP64 log-amplitudes within 1e-9 absolute with equal signs, local
 energies within 1e-8 relative, replayed sweeps bit-exact in configurations and
 acceptance counts; FP32 amplitudes within 5e-6 * |top| |bottom| (the norm
 product bounds the final overlap's cancellation; FP32 Jacobi eigenvectors
-carry ~1e-6 / relative gap)."""
+carry ~1e-7 / relative gap; measured <= 2.4e-7)."""
 import numpy as np
 import pytest
 import torch

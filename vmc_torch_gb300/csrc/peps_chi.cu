@@ -221,6 +221,115 @@ __device__ void warp_hestenes(T (&u)[32], T* V, T* lam) {
   __syncwarp();
 }
 
+// One warp: the left singular vectors of a block A (lane i holds row i, nq
+// <= 32 columns, rows beyond the block zero) by a pivoted LQ factorisation
+// A = L Q followed by one-sided Jacobi on the rows of L^T (Drmac & Veselic:
+// Jacobi on the triangular factor of a pivoted QR converges in about half the
+// sweeps).  LQ: Householder reflectors from the right, the pivot row of step
+// k the unprocessed row with the largest trailing norm (rows stay in their
+// lanes; the order only decides which row defines reflector k).  Then L^T
+// goes through shared memory (lane k holds column k of L), its rows are made
+// orthogonal (no rotation matrix is kept: A A^T = L L^T, whose eigenvectors
+// are the normalised final rows), and lam[k] = |row k|^2, V[k * 33 + i] =
+// row k / |row k| (zero for a zero row).  S: a 32 x 33 scratch.
+template <typename T>
+__device__ void warp_lq_jacobi(T (&u)[32], int nq, T* S, T* V, T* lam) {
+  const int ln = threadIdx.x & 31;
+  bool done = false;
+  for (int k = 0; k < nq; ++k) {
+    T nr = T(0);
+#pragma unroll
+    for (int j = 0; j < 32; ++j) nr = (j >= k) ? fma(u[j], u[j], nr) : nr;
+    // pivot: the unprocessed row with the largest trailing norm (ties: lower lane)
+    T key = done ? T(-1) : nr;
+    int p = ln;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const T ok = __shfl_xor_sync(VMC_FULL_MASK, key, o);
+      const int op = __shfl_xor_sync(VMC_FULL_MASK, p, o);
+      if (ok > key || (ok == key && op < p)) { key = ok; p = op; }
+    }
+    const T pn = __shfl_sync(VMC_FULL_MASK, nr, p);
+    if (!(pn > T(0))) break;   // the remaining rows vanish: A is rank k
+    if (ln == p) done = true;
+    // reflector v from the pivot row's trailing part: v = x - alpha e_k, alpha = -sign(x_k) |x|
+    T v[32];
+#pragma unroll
+    for (int j = 0; j < 32; ++j) v[j] = (j >= k) ? __shfl_sync(VMC_FULL_MASK, u[j], p) : T(0);
+    T vk = T(0);
+#pragma unroll
+    for (int j = 0; j < 32; ++j) vk = (j == k) ? v[j] : vk;
+    const T alpha = (vk >= T(0)) ? -sqrt(pn) : sqrt(pn);
+    const T vk2 = vk - alpha;
+    const T vv = pn - vk * vk + vk2 * vk2;
+#pragma unroll
+    for (int j = 0; j < 32; ++j) v[j] = (j == k) ? vk2 : v[j];
+    T d = T(0);
+#pragma unroll
+    for (int j = 0; j < 32; ++j) d = fma(u[j], v[j], d);
+    const T f = T(2) * d / vv;
+#pragma unroll
+    for (int j = 0; j < 32; ++j) u[j] = fma(-f, v[j], u[j]);
+  }
+  // L^T: lane k takes column k of L
+  __syncwarp();
+#pragma unroll
+  for (int j = 0; j < 32; ++j) S[ln * 33 + j] = u[j];
+  __syncwarp();
+#pragma unroll
+  for (int j = 0; j < 32; ++j) u[j] = S[j * 33 + ln];
+  __syncwarp();
+  const T tol = std::is_same<T, float>::value ? T(2e-7) : T(4e-16);
+  T nrm = T(0);
+#pragma unroll
+  for (int j = 0; j < 32; ++j) nrm = fma(u[j], u[j], nrm);
+  T floor_ = nrm;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) floor_ = fmax(floor_, __shfl_xor_sync(VMC_FULL_MASK, floor_, o));
+  floor_ *= tol;
+  for (int sw = 0; sw < 20; ++sw) {
+    bool rotated = false;
+    for (int m = 1; m < 32; ++m) {
+      const bool lead = ln < (ln ^ m);
+      T o[32];
+      T gam = T(0), alp = T(0);
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {
+        o[j] = __shfl_xor_sync(VMC_FULL_MASK, u[j], m);
+        gam = fma(u[j], o[j], gam);
+        alp = fma(u[j], u[j], alp);
+      }
+      const T bet = __shfl_xor_sync(VMC_FULL_MASK, alp, m);
+      T c = T(1), s = T(0);
+      int need = 0;
+      if (lead && fabs(gam) > floor_ && fabs(gam) > tol * sqrt(alp * bet)) {
+        const T zeta = (bet - alp) / (T(2) * gam);
+        const T t = (zeta >= T(0) ? T(1) : T(-1)) / (fabs(zeta) + hypot(T(1), zeta));
+        c = T(1) / sqrt(T(1) + t * t);
+        s = t * c;
+        need = 1;
+      }
+      const T c2 = __shfl_xor_sync(VMC_FULL_MASK, c, m), s2 = __shfl_xor_sync(VMC_FULL_MASK, s, m);
+      const int n2 = __shfl_xor_sync(VMC_FULL_MASK, need, m);
+      if (!lead) { c = c2; s = s2; need = n2; }
+      if (!__any_sync(VMC_FULL_MASK, need)) continue;
+      rotated = true;
+      const T sp = lead ? -s : s;
+#pragma unroll
+      for (int j = 0; j < 32; ++j) u[j] = fma(sp, o[j], c * u[j]);
+    }
+    if (!rotated) break;
+  }
+  nrm = T(0);
+#pragma unroll
+  for (int j = 0; j < 32; ++j) nrm = fma(u[j], u[j], nrm);
+  lam[ln] = nrm;
+  const T inv = nrm > T(0) ? T(1) / sqrt(nrm) : T(0);
+#pragma unroll
+  for (int j = 0; j < 32; ++j) V[ln * 33 + j] = u[j] * inv;
+  __syncwarp();
+}
+
 // Largest |x| of the CTA (thread 0's value is returned to every thread).
 template <typename T>
 __device__ T cta_absmax(T m, T* red) {
@@ -523,7 +632,7 @@ __global__ void __launch_bounds__(32 * 2 * CHI_TRUNC_ITEMS)
 #pragma unroll
     for (int j = 0; j < 32; ++j)
       u[j] = (on && ln < nb && j < nq) ? st[at(pi, block_member<D>(qcls, j))] : T(0);
-    warp_hestenes<T>(u, V, lam + b * 32);
+    warp_lq_jacobi<T>(u, nq, S, V, lam + b * 32);
   } else {
     // Gram block: lane i accumulates row i
     T acc[32];
@@ -543,15 +652,17 @@ __global__ void __launch_bounds__(32 * 2 * CHI_TRUNC_ITEMS)
   }
   __syncthreads();
   {
+    // eigenpairs: lanes < nq (rows of L^T) on the one-sided path, < nb on the Gram path
+    const int nval = ONE_SIDED ? nq : nb;
     const T l = lam[b * 32 + ln];
     int rank = 0;
     for (int e = 0; e < 64; ++e) {
       const int b2 = e >> 5, i2 = e & 31;
-      if (i2 >= nb) continue;
+      if (i2 >= nval) continue;
       const T l2 = lam[e];
       rank += (l2 > l) || (l2 == l && (b2 < b || (b2 == b && i2 < ln)));
     }
-    keep[b * 32 + ln] = (ln < nb) && rank < sc.chi;
+    keep[b * 32 + ln] = (ln < nval) && rank < sc.chi;
   }
   __syncwarp();
   // projection of the block onto the kept eigenvectors, one big-side column at a time
