@@ -404,14 +404,27 @@ __device__ __forceinline__ int table_entry(int ti, int ia, int ib, int px, int s
 }
 
 // One column of a row absorption, in place on W[h][idx] (all threads).
-// par: electron parity absorbed before this column; px: the site's.
+// par: electron parity absorbed before this column; px: the site's.  The
+// first half of the CTA takes the groups of parity class 0, the second half
+// class 1 (class = par + digit parity of the group's other digits), so each
+// warp works on one class and keeps that class's (D^2/2)^2 block of the site
+// tensor in registers for the whole column.
 template <typename T, int D>
 __device__ void column_forward(T* W, int NS, int stride, int par, int px, const T* Ac) {
   constexpr int H = D * D / 2;
-  for (int gi = threadIdx.x; gi < NS / D; gi += blockDim.x) {
-    const int lo = gi % stride, hi = gi / stride;
+  const int half = (int)blockDim.x >> 1;
+  const int ti = threadIdx.x < half ? 0 : 1, tl = threadIdx.x - ti * half, to = ti ^ px;
+  T A[H * H];
+#pragma unroll
+  for (int k = 0; k < H * H; ++k) A[k] = Ac[ti * H * H + k];
+  const int G = NS / D, Gh = (G + 1) >> 1;
+  for (int i = tl; i < Gh; i += half) {
+    // the i-th group of the class: other-digit index with digit parity ti ^ par
+    const uint32_t e = (uint32_t)i << 1;
+    const int g = (int)(e | (uint32_t)((ti ^ par ^ digit_parity<D>(e)) & 1));
+    if (g >= G) continue;
+    const int lo = g % stride, hi = g / stride;
     const int base = hi * stride * D + lo;
-    const int ti = (par ^ digit_parity<D>((uint32_t)base)) & 1, to = ti ^ px;
     T in[H];
     bool any = false;
 #pragma unroll
@@ -422,14 +435,13 @@ __device__ void column_forward(T* W, int NS, int stride, int par, int px, const 
       any |= in[ia] != T(0);
     }
     if (!any) continue;
-    const T* Ab = Ac + ti * H * H;
     T outv[H];
 #pragma unroll
     for (int ib = 0; ib < H; ++ib) outv[ib] = T(0);
 #pragma unroll
     for (int ia = 0; ia < H; ++ia)
 #pragma unroll
-      for (int ib = 0; ib < H; ++ib) outv[ib] += in[ia] * Ab[ia * H + ib];
+      for (int ib = 0; ib < H; ++ib) outv[ib] += in[ia] * A[ia * H + ib];
     if (px) {  // the input class empties
 #pragma unroll
       for (int ia = 0; ia < H; ++ia) {
