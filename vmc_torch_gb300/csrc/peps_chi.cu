@@ -586,7 +586,7 @@ __global__ void __launch_bounds__(CHI_NT)
   if (threadIdx.x == 0) expo_io[slot] = bad ? CHI_EXP_BAD : (zero ? CHI_EXP_ZERO : expo);
 }
 
-constexpr int CHI_TRUNC_ITEMS = 4;  // items per CTA, two warps (one per parity block) each
+constexpr int CHI_TRUNC_ITEMS = 2;  // items per CTA, two warps (one per parity block) each
 
 template <typename T>
 struct ChiTruncSmem {
