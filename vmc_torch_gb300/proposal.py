@@ -294,7 +294,7 @@ class OnlineProposalTraining:
     accumulates the training time for the ESS accounting, measured like the
     samplers' times: CUDA events on the current stream around each session."""
 
-    def __init__(self, proposal, model, every=10, epochs=2, batch=4096, then=None):
+    def __init__(self, proposal, model, every=10, epochs=4, batch=16384, then=None):
         self.proposal, self.model = proposal, model
         self.every, self.epochs, self.batch = int(every), int(epochs), int(batch)
         self.then = then
