@@ -31,6 +31,13 @@
  *   vmc_peps_eval / _sweep /     — fPEPS_Model_GPU.amplitude / log_amplitude,
  *   _local_energy                  vmc_torch/GPU/models/pureTNS.py:82-146, driven by
  *                                  the same sampler and energy loop as the other models
+ *                                  (exact contraction: max_bond absent or large)
+ *   vmc_peps_chi_*               — the same with the boundaries truncated to max_bond
+ *                                  (contract_boundary_from_xmin_/xmax_ with max_bond = chi,
+ *                                  pureTNS.py:100-111), and its log-derivatives
+ *   vmc_split_bf16x3 /           — the Gram matrix lpg_scaled @ lpg_scaled.T of
+ *   vmc_sr_gram_tc                 minSR_solver_gpu (vmc_torch/GPU/optimizer.py:551-553)
+ *                                  on the tensor cores
  *   vmc_sym_*                    — FermionSymmetryProjectedModel,
  *                                  vmc_torch/GPU/models/symmetry.py:673-1136
  *   vmc_propose_edge / _accept_edge, vmc_conn_rows, vmc_eloc_*
