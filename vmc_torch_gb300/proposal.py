@@ -16,7 +16,7 @@ are kept in a ring buffer on the device.
 
 No reference counterpart: the reference samples with local exchange / hop moves
 only (vmc_torch/GPU/sampler.py:47-137); plain Metropolis stays available as the
-fallback and as the baseline that judges this proposal (tau_int of E_loc).
+fallback and as the baseline this proposal is measured against (tau_int of E_loc).
 """
 import math
 import time
