@@ -412,6 +412,32 @@ def logamp_grad_chi(T, x, chi):
     return Tt.grad.numpy()
 
 
+def trunc_adjoint(M, B, k):
+    """Cotangent of the rank-k truncation P(M) = U_k S_k V_k^T against B:
+    d<P(M), B> = <dM, Mbar> with
+        Mbar = P_k B + sum_{i < k <= j} w_ij (q_j u_i^T + q_i u_j^T),
+        w_ij = (q_j^T B u_i + q_i^T B u_j) / (s_i^2 - s_j^2),
+    q the left singular vectors, u_i = s_i v_i (the first-order change of the
+    kept singular subspace).  The formula vmc_peps_chi_logpsi_grad evaluates
+    per parity block (FP64 numpy here, test infrastructure)."""
+    u, sv, vh = np.linalg.svd(M)
+    n = sv.size
+    Q = u[:, :n].T                     # rows q_i
+    U = sv[:, None] * vh[:n]           # rows u_i = s_i v_i
+    lam = sv ** 2
+    C = Q @ B
+    X = C @ U.T                        # X[a][c] = q_a^T B u_c
+    keep = np.arange(n) < k
+    R = keep[:, None] * C
+    for a in range(n):
+        for c in range(n):
+            if keep[a] == keep[c]:
+                continue
+            den = (lam[a] - lam[c]) if keep[a] else (lam[c] - lam[a])
+            R[a] = R[a] + (X[a, c] + X[c, a]) / den * U[c]
+    return Q.T @ R
+
+
 def logamp(T, X, method="rows", chi=None):
     if method == "chi":
         a = np.array([amp_state_chi(T, x, chi) for x in np.asarray(X)])

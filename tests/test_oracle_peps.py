@@ -88,3 +88,23 @@ def test_chi_gradient_oracle_matches_finite_differences():
         Tm[idx] -= h
         fd = (np.log(abs(peps.amp_state_chi(Tp, x, 8))) - np.log(abs(peps.amp_state_chi(Tm, x, 8)))) / (2 * h)
         assert abs(fd - g[idx]) <= 1e-5 * max(abs(fd), 1e-3)
+
+
+@pytest.mark.parametrize("n,k", [(32, 8), (16, 5), (8, 3)])
+def test_truncation_adjoint_formula(n, k):
+    """The cotangent of the rank-k truncation (the formula of the chi
+    log-derivative kernels) against central differences of <P(M), B>."""
+    rng = np.random.default_rng(n + k)
+    M = rng.normal(size=(n, n)) * np.exp(-0.3 * np.arange(n))[:, None]
+    B = rng.normal(size=(n, n))
+    Mbar = peps.trunc_adjoint(M, B, k)
+
+    def f(Mx):
+        u, s, vh = np.linalg.svd(Mx)
+        return float(np.sum(((u[:, :k] * s[:k]) @ vh[:k]) * B))
+
+    for _ in range(3):
+        dM = rng.normal(size=(n, n))
+        h = 1e-6
+        fd = (f(M + h * dM) - f(M - h * dM)) / (2 * h)
+        assert abs(np.sum(dM * Mbar) - fd) <= 1e-6 * max(1.0, abs(fd))
