@@ -19,18 +19,22 @@
 // (their truncation is the identity).  At 6x6, D = 4, chi = 16 each side
 // truncates only the middle cut, once.
 //
-// Truncation at cut k: the state as a matrix M (D^k x D^(Ly-k)); on its
-// smaller side the Gram matrix (M M^T or M^T M) is block-diagonal in the Z2
-// parity of the index (each tensor is parity-even), so two blocks of at most
-// 32 x 32.  One warp per block diagonalises it by cyclic Jacobi (pairs
-// (i, i xor m), m = 1..31: every pair once per sweep, 16 disjoint rotations a
-// round; lane i holds row i of the matrix and eigenvector i in registers; the
-// column half of each two-sided rotation goes through one transpose in shared
-// memory).  The chi largest eigenvalues over both blocks select the kept
-// eigenvectors U and the state becomes U U^T M.  This equals the SVD
-// truncation because the retained singular vectors are the Gram's top
-// eigenvectors; precision "fp64" runs everything in FP64, "fp32" the state,
-// Gram and Jacobi in FP32 with FP64 accumulation of the final overlap.
+// Truncation at cut k: the state as a matrix M (D^k x D^(Ly-k)) is
+// block-diagonal in the Z2 parity of its smaller side's index (each tensor is
+// parity-even), two blocks of at most 32 rows, one warp per block.  When a
+// block also has at most 32 columns (the middle cut of a 6-wide lattice): a
+// pivoted LQ factorisation in the warp, then one-sided Jacobi on the rows of
+// L^T (pairs (i, i xor m), m = 1..31: every pair once per sweep, 16 disjoint
+// rotations a round), whose normalised final rows are the block's left
+// singular vectors.  Otherwise the block's Gram matrix by two-sided Jacobi.
+// The chi largest singular values over both blocks select the kept vectors U
+// and the state becomes U U^T M, the SVD truncation.  Precision "fp64" runs
+// everything in FP64, "fp32" the state and the Jacobi in FP32 with FP64
+// accumulation of the final overlap.
+//
+// Log-derivatives: the cotangent of each side's truncation against the other
+// side's truncated state (first-order change of the kept singular subspace),
+// then a reverse row sweep over recomputed forward column states.
 //
 // After every absorbed row the state is rescaled by a power of two (exact)
 // and the exponent accumulated, so FP32 does not overflow.
