@@ -1,7 +1,9 @@
 // Sample-space SR (minSR) linear algebra on one GPU:
-//   column means and centring/scaling of O, the Gram matrix T = O~ O~^T + lambda I,
-//   a blocked right-looking FP64 Cholesky of T, forward/backward substitution,
-//   and dp = O~^T x.  Also the plain energy gradient <E O> - <E><O>.
+//   column means and centring/scaling of O, the Gram matrix T = O~ O~^T + lambda I
+//   on the CUDA cores (the tensor-core Gram is in gram.cu), a blocked right-looking
+//   Cholesky of T (FP64 tiles and panels, double-float trailing updates), blocked
+//   forward/backward substitution, and dp = O~^T x.  Also the plain energy
+//   gradient <E O> - <E><O>.
 #include "common.cuh"
 
 namespace {
